@@ -1,0 +1,80 @@
+/*
+ * C ABI of the GB300 quaternion eigensolver (libzquatev_gb300.so).
+ *
+ * A quaternion-Hermitian matrix H = (A -B*; B A*) of order n2 = 2n (A Hermitian,
+ * B complex antisymmetric) is passed as a column-major n2 x ld2 array of
+ * complex doubles (interleaved re, im). Only its left half [A; B] is read. On
+ * return the array holds all n2 eigenvectors in the (U -V*; V U*) layout and
+ * eig[0..n-1] the ascending eigenvalues (each is doubly degenerate; columns i
+ * and i+n belong to eig[i]); eig[n..] is not touched.
+ *
+ * Return codes: 0 success; -1 bad n2 (odd or negative); -2 null D; -3 ld2 < n2;
+ * -4 null eig; -5 other bad argument; -100 CUDA failure; -101 out of device
+ * memory; -103 size above the fixed limit of the called entry point.
+ * zq_last_error() describes the last failure on the calling thread.
+ */
+#ifndef ZQUATEV_GB300_H
+#define ZQUATEV_GB300_H
+
+#ifdef __cplusplus
+#include <complex>
+extern "C" {
+#endif
+
+/* Replaces ts::zquatev(n2, D, ld2, eig) (reference zquatev.h:54,
+ * zquatev.cc:42-100) for FFI callers: same arguments with D as interleaved
+ * doubles in HOST memory. Unlike the reference, ld2 > n2 is handled (V is
+ * stored at rows n..2n-1; reference quirk at zquatev.cc:84-90). */
+int zquatev_c(int n2, double* D, int ld2, double* eig);
+
+/* Eigenvalues only (jobz = 'N'): the reference always computes vectors
+ * (zquatev.cc:84, blocked.cc:477-544); this skips Q formation and the
+ * back-transform. D (host) is used as scratch; eig[0..n-1] receives the values. */
+int zquatev_values(int n2, double* D, int ld2, double* eig);
+
+/* Device-pointer variant of ts::zquatev (zquatev.h:54): dD is an n2 x ld2
+ * complex array in DEVICE memory, deig >= n doubles in device memory. The work
+ * is ordered after `stream` (a cudaStream_t, 0 = legacy default stream) and the
+ * call returns without synchronising. */
+int zquatev_device(int n2, double* dD, int ld2, double* deig, void* stream);
+
+/* Device-pointer eigenvalues-only variant. */
+int zquatev_values_device(int n2, double* dD, int ld2, double* deig, void* stream);
+
+/* Real symmetric tridiagonal eigensolver (the stage that replaces zhbev at
+ * zquatev.cc:74-84): d (n), e (n-1, the off-diagonal), lam (n, ascending) and
+ * Z (n x ldz, column-major eigenvectors) all in device memory. */
+int zq_stedc_device(int n, const double* d, const double* e, double* lam, double* Z, int ldz, void* stream);
+
+/* Batched solve of `count` independent matrices held in device memory:
+ * matrix b has order n2s[b] (even), starts at dD + 2*offs[b] doubles
+ * (complex offset offs[b]) with leading dimension ld2s[b], and eigenvalues at
+ * deig + eoffs[b]. All arrays n2s/ld2s/offs/eoffs are HOST arrays. The whole
+ * batch runs as one persistent kernel launch ordered after `stream`.
+ * No reference counterpart (the reference solves one matrix per call). */
+int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const long long* offs,
+                           const long long* eoffs, double* dD, double* deig, void* stream);
+
+/* Panel width of the blocked tridiagonalisation (the reference hard-codes
+ * nb = 20 at zquatev.cc:64). Valid range 1..64; default 32. */
+int zq_set_block_size(int nb);
+int zq_get_block_size(void);
+
+/* Frees the cached device workspace of the current device. */
+int zq_release_workspace(void);
+
+const char* zq_last_error(void);
+int zq_version(void);
+
+#ifdef __cplusplus
+} /* extern "C" */
+
+/* The reference's own C++ entry point, exported with the same mangled name
+ * (_ZN2ts7zquatevEiPSt7complexIdEiPd), so programs linked against the
+ * reference link against this library unchanged (zquatev.h:54). */
+namespace ts {
+int zquatev(const int n2, std::complex<double>* const D, const int ld2, double* const eig);
+}
+#endif
+
+#endif /* ZQUATEV_GB300_H */

@@ -1,0 +1,200 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracles.
+
+Oracles: the reference's own outputs (golden fixtures from the compiled
+reference), the numpy restatement oracle/port.py, and FP64 eigh on the full
+2n x 2n Hermitian matrix. Tolerances (from the task's accuracy bar):
+eigenvalues within 1e-12 * ||H||_2; residual max_j ||H v_j - lambda_j v_j|| /
+||H||_2 <= 1e-12; orthonormality max |V^H V - I| <= 1e-12; the (U -V*; V U*)
+structure exact bit for bit; eigenvector subspaces per eigenvalue cluster
+within 1e-8 (sin of the largest principal angle, gap-dependent).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import port
+from zquatev_gb300 import _lib, inputs, metrics, solver
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def run(d, n2=None, ld2=None, sentinel=7.25):
+    out = np.array(d, dtype=np.complex128, order="F", copy=True)
+    n2 = out.shape[1] if n2 is None else n2
+    ld2 = out.shape[0] if ld2 is None else ld2
+    eig = np.full(max(n2, 1), sentinel)
+    rc = solver.zquatev(n2, out, ld2, eig)
+    assert rc == 0, (rc, _lib.last_error())
+    return out, eig
+
+
+def check_solution(d, out, eig, n, ref_eig=None):
+    h = inputs.full_from_blocks(d[:n, :n], d[n:2 * n, :n])
+    if ref_eig is None:
+        ref_eig = np.linalg.eigvalsh(h)[::2]
+    hn = metrics.h_norm2(ref_eig)
+    v = out[:2 * n, :2 * n]
+    assert metrics.eig_error(eig[:n], ref_eig, hn) <= TOL
+    assert metrics.residual(h, v, eig[:n]) <= TOL
+    assert metrics.orthonormality(v) <= TOL
+    assert metrics.structure_exact(out, n)
+    assert np.all(np.diff(eig[:n]) >= 0)
+    return h
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_against_reference_golden(gpu, path):
+    z = np.load(path)
+    left = z["left"]
+    n = left.shape[1]
+    d = np.zeros((2 * n, 2 * n), dtype=np.complex128, order="F")
+    d[:, :n] = left
+    d[:, n:] = 3.0 - 1.0j  # right half is ignored by the solver
+    out, eig = run(d)
+    assert np.all(eig[n:] == 7.25)  # eig[n..] untouched (reference behaviour)
+    check_solution(d, out, eig, n, ref_eig=z["eig"])
+    tol = 1e-6 * max(metrics.h_norm2(z["eig"]), 1.0)
+    assert metrics.subspace_distance(out, eig[:n], z["out"], z["eig"], tol) < 1e-8
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 20, 21, 22, 31, 32, 33, 63, 64, 65, 97, 128, 200])
+def test_random_sizes(gpu, n):
+    d = inputs.random_matrix(n, 300 + n)
+    out, eig = run(d)
+    check_solution(d, out, eig, n)
+
+
+@pytest.mark.parametrize("nb", [1, 2, 8, 16, 32, 64])
+def test_panel_widths(gpu, nb):
+    assert gpu.zq_set_block_size(nb) == 0
+    try:
+        n = 150
+        d = inputs.random_matrix(n, 77)
+        out, eig = run(d)
+        check_solution(d, out, eig, n)
+    finally:
+        gpu.zq_set_block_size(32)
+
+
+def test_against_port_config0(gpu):
+    """n2 = 512 random matrix: GPU vs the numpy restatement of the reference."""
+    n = 256
+    d = inputs.random_matrix(n, 2024)
+    out, eig = run(d)
+    pd = d.copy(order="F")
+    pe = np.zeros(2 * n)
+    assert port.zquatev(2 * n, pd, 2 * n, pe) == 0
+    h = check_solution(d, out, eig, n, ref_eig=pe[:n])
+    tol = 1e-6 * metrics.h_norm2(pe[:n])
+    assert metrics.subspace_distance(out, eig[:n], pd, pe[:n], tol) < 1e-8
+    assert metrics.residual(h, pd, pe[:n]) < 1e-12
+
+
+def test_leading_dimension_larger(gpu):
+    n = 40
+    d0 = inputs.random_matrix(n, 5)
+    d = inputs.random_matrix(n, 5, ld2=2 * n + 6)
+    d[2 * n:, :] = 123.0  # padding rows must not be read or written
+    out, eig = run(d, n2=2 * n, ld2=2 * n + 6)
+    assert np.all(out[2 * n:, :] == 123.0)
+    check_solution(d0, out[:2 * n], eig, n)
+
+
+def test_clustered_spectrum(gpu):
+    n = 160
+    d, lam = inputs.clustered_matrix(n, 11)
+    out, eig = run(d)
+    h = check_solution(d, out, eig, n, ref_eig=np.sort(lam))
+    w, vref = np.linalg.eigh(h)
+    # compare invariant subspaces of the 1e-6-wide clusters
+    order = np.argsort(w)
+    vr = np.zeros_like(vref)
+    vr[:, :n] = vref[:, order[::2]]
+    vr[:, n:] = vref[:, order[1::2]]
+    # Kramers partners of eigh are arbitrary within each double eigenvalue; use both
+    assert metrics.subspace_distance(out, eig[:n], vref[:, np.argsort(w)][:, list(range(0, 2 * n, 2)) + list(range(1, 2 * n, 2))],
+                                     np.sort(w)[::2], 1e-4) < 1e-6
+
+
+def test_values_only(gpu):
+    n = 90
+    d = inputs.random_matrix(n, 8)
+    scratch = d.copy(order="F")
+    eig = np.zeros(2 * n)
+    assert solver.eigvals(2 * n, scratch, 2 * n, eig) == 0
+    h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
+    ref = np.linalg.eigvalsh(h)[::2]
+    assert metrics.eig_error(eig[:n], ref, metrics.h_norm2(ref)) <= TOL
+
+
+def test_repeated_and_mixed_sizes(gpu):
+    """Workspace and plan caching across calls of different sizes."""
+    for n in [50, 10, 120, 50, 1, 64]:
+        d = inputs.random_matrix(n, 1000 + n)
+        out, eig = run(d)
+        check_solution(d, out, eig, n)
+
+
+def test_device_api_torch(gpu):
+    import torch
+
+    n = 70
+    d = inputs.random_matrix(n, 21)
+    # column-major (ld2, n2) == row-major (n2, ld2) of the transpose
+    dt = torch.from_numpy(np.ascontiguousarray(d.T)).cuda()
+    de = torch.zeros(2 * n, dtype=torch.float64, device="cuda")
+    rc = solver.zquatev_device(dt, de)
+    assert rc == 0
+    torch.cuda.synchronize()
+    out = np.asfortranarray(dt.cpu().numpy().T)
+    check_solution(d, out, de.cpu().numpy(), n)
+
+
+@pytest.mark.parametrize("kind", ["random", "wilkinson", "zero_offdiag", "degenerate", "clustered"])
+def test_stedc(gpu, kind):
+    import torch
+
+    rng = np.random.default_rng(5)
+    n = 300
+    if kind == "random":
+        dd, ee = rng.standard_normal(n), np.abs(rng.standard_normal(n - 1))
+    elif kind == "wilkinson":
+        dd, ee = np.abs(np.arange(n) - n // 2).astype(float), np.ones(n - 1)
+    elif kind == "zero_offdiag":
+        dd, ee = rng.standard_normal(n), np.abs(rng.standard_normal(n - 1))
+        ee[::7] = 0.0
+    elif kind == "degenerate":
+        dd, ee = np.ones(n), np.full(n - 1, 1e-30)
+    else:
+        import scipy.linalg as sl
+
+        lam = inputs.clustered_spectrum(n, 3)
+        q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        t = sl.hessenberg((q * lam) @ q.T)
+        dd, ee = np.diag(t).copy(), np.abs(np.diag(t, -1)).copy()
+    t = np.diag(dd) + np.diag(ee, 1) + np.diag(ee, -1)
+    d_ = torch.tensor(dd, device="cuda")
+    e_ = torch.tensor(ee, device="cuda")
+    lam = torch.zeros(n, dtype=torch.float64, device="cuda")
+    z = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    assert solver.stedc_device(d_, e_, lam, z) == 0
+    torch.cuda.synchronize()
+    w = lam.cpu().numpy()
+    zz = z.cpu().numpy().T  # column-major
+    ref = np.linalg.eigvalsh(t)
+    tn = max(np.abs(ref).max(), 1e-300)
+    assert np.max(np.abs(w - ref)) / tn < 1e-13
+    assert np.max(np.linalg.norm(t @ zz - zz * w, axis=0)) / tn < 1e-13
+    assert np.max(np.abs(zz.T @ zz - np.eye(n))) < 1e-13
+
+
+def test_larger_random(gpu):
+    n = 1024
+    d = inputs.random_matrix(n, 4242)
+    out, eig = run(d)
+    check_solution(d, out, eig, n)

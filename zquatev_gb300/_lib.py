@@ -1,0 +1,65 @@
+"""ctypes binding of libzquatev_gb300.so (the C ABI in include/zquatev_gb300.h).
+
+The library is built in-tree by zquatev_gb300.build. Loading fails loudly if it
+is missing: there is no CPU fallback anywhere in this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libzquatev_gb300.so")
+
+_c_int, _c_ll, _vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p
+
+# name -> (restype, argtypes); every entry point declared in include/zquatev_gb300.h
+SIGNATURES = {
+    "zquatev_c": (_c_int, [_c_int, _vp, _c_int, _vp]),
+    "zquatev_values": (_c_int, [_c_int, _vp, _c_int, _vp]),
+    "zquatev_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
+    "zquatev_values_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
+    "zq_stedc_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),
+    "zquatev_batched_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "zq_set_block_size": (_c_int, [_c_int]),
+    "zq_get_block_size": (_c_int, []),
+    "zq_release_workspace": (_c_int, []),
+    "zq_last_error": (ctypes.c_char_p, []),
+    "zq_version": (_c_int, []),
+}
+# the reference's C++ symbol ts::zquatev(int, std::complex<double>*, int, double*)
+REFERENCE_SYMBOL = "_ZN2ts7zquatevEiPSt7complexIdEiPd"
+
+_lib = None
+
+
+class ZquatevError(RuntimeError):
+    pass
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ZquatevError(f"{LIB_PATH} is not built; run zquatev_gb300.build.build() first")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        ref = getattr(lib, REFERENCE_SYMBOL)
+        ref.restype = _c_int
+        ref.argtypes = [_c_int, _vp, _c_int, _vp]
+        _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    msg = load().zq_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int, what: str) -> int:
+    if rc < 0:
+        raise ZquatevError(f"{what} returned {rc}: {last_error()}")
+    return rc

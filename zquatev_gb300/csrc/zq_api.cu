@@ -1,0 +1,378 @@
+// Host orchestration and the C ABI of the GB300 quaternion eigensolver.
+//
+// Drop-in for ts::zquatev (zquatev.h:54, zquatev.cc:42-100): same symbol, same
+// arguments, same output layout. Per call:
+//   H1  copy the left half [A; B] of D to the device           (zquatev.cc:47-54)
+//   H4-H13 blocked quaternion tridiagonalisation (zq_tridiag.cu)  (zquatev.cc:68-72)
+//   H14 phase reduction + D&C tridiagonal eigensolver (zq_stedc.cu) (zquatev.cc:74-84)
+//   H12/H15 Q Phi formed from the stored reflectors, concurrently with the D&C
+//       on a second stream, then (U; V) = (Q Phi) Z    (zquatev.cc:86-90)
+//   H16 symmetry fill of the right half on the device    (zquatev.cc:92-98)
+//   copy all of D and eig[0..n-1] back.
+// H2/H3 (Q init, workspace) become device buffers owned by a per-device
+// context; H17 (SuperMatrix, transpose helpers) has no counterpart.
+//
+// Differences from the reference, all deliberate:
+//   * ld2 > n2 works (V is written at rows n..2n-1; the reference writes it at
+//     row ld2/2 and reads the input at row n, zquatev.cc:52-53 vs :84,:90);
+//   * argument errors return negative codes instead of asserting (zquatev.cc:43);
+//   * eig[n..] is left untouched, as in the reference.
+#include "zq_common.cuh"
+#include "zq_kernels.h"
+#include "../../include/zquatev_gb300.h"
+
+#include <complex>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace zq {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(cudaError_t e, const char* what, const char* file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  g_last_error = buf;
+}
+const char* last_error_message() { return g_last_error.c_str(); }
+static void set_msg(const char* m) { g_last_error = m; }
+
+// ----------------------------------------------------------------------------
+// per-device context: streams, events, growable workspace, cached D&C plan
+// ----------------------------------------------------------------------------
+struct Context {
+  int device = -1;
+  cudaStream_t st = nullptr, st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  int dc_n = -1;
+  DcPlan dc;
+  std::mutex mu;
+};
+
+static std::mutex g_ctx_mu;
+static Context* g_ctx[64];
+static int g_nb = 32;   // panel width (autotuned table may override per n)
+static int g_nbq = 32;  // Q-formation block
+
+static int nb_for(int n) {
+  if (const char* s = getenv("ZQ_NB")) { const int v = atoi(s); if (v >= 1 && v <= 64) return v; }
+  (void)n;
+  return g_nb;
+}
+
+static int get_context(Context** out) {
+  int dev = 0;
+  ZQ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { set_msg("device ordinal out of range"); return ZQ_ERR_ARG; }
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  if (!g_ctx[dev]) {
+    Context* c = new Context();
+    c->device = dev;
+    ZQ_CUDA(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    ZQ_CUDA(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
+    ZQ_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    ZQ_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    g_ctx[dev] = c;
+  }
+  *out = g_ctx[dev];
+  return ZQ_OK;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// workspace layout for one solve of quaternion size n (excluding the output D)
+struct Layout {
+  size_t tri, small, dc, fq, nodes, descs, total;
+};
+static Layout layout_for(int n, int nbmax, int nbq, size_t nnodes, size_t ndescs) {
+  Layout L{};
+  L.tri = align256(tridiag_workspace_bytes<double>(n, nbmax));
+  L.small = align256(sizeof(double) * (size_t)(n + 4 * (size_t)n + n + n + 4 * (size_t)n + n + 16));
+  L.dc = align256(sizeof(double) * DcPlan::workspace_doubles(n));
+  L.fq = align256(form_q_workspace_bytes(n, nbq));
+  L.nodes = align256(sizeof(DcNode) * (nnodes + 1));
+  L.descs = align256(sizeof(DgemmDesc) * (ndescs + 2));
+  L.total = L.tri + L.small + L.dc + L.fq + L.nodes + L.descs;
+  return L;
+}
+
+static int ensure_ws(Context* c, size_t bytes) {
+  if (c->ws_bytes >= bytes) return ZQ_OK;
+  if (c->ws) { cudaStreamSynchronize(c->st); cudaStreamSynchronize(c->st2); cudaFree(c->ws); c->ws = nullptr; c->ws_bytes = 0; }
+  ZQ_CUDA(cudaMalloc(&c->ws, bytes));
+  c->ws_bytes = bytes;
+  c->dc_n = -1;  // plan pointers refer to the old buffer
+  return ZQ_OK;
+}
+
+// Solve on device data. dD: n2 x n2 complex (ld ldd) whose left half holds [A; B];
+// on return dD holds the eigenvectors and deig[0..n-1] the eigenvalues.
+struct StageTimer {
+  bool on = false;
+  cudaEvent_t ev[8];
+  const char* names[8];
+  int k = 0;
+  explicit StageTimer(bool enable) : on(enable) {
+    if (on) for (int i = 0; i < 8; ++i) cudaEventCreate(&ev[i]);
+  }
+  void mark(const char* name, cudaStream_t st) {
+    if (!on || k >= 8) return;
+    names[k] = name;
+    cudaEventRecord(ev[k++], st);
+  }
+  ~StageTimer() {
+    if (!on) return;
+    cudaEventSynchronize(ev[k - 1]);
+    for (int i = 1; i < k; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
+      fprintf(stderr, "[zq] %-12s %9.3f ms\n", names[i], ms);
+    }
+    for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+  }
+};
+
+static int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool vectors, cudaStream_t st) {
+  const int nb = nb_for(n);
+  const char* tenv = getenv("ZQ_TIMING");
+  StageTimer tm(tenv && tenv[0] == '1');
+  const int nbq = g_nbq;
+  if (c->dc_n != n) {
+    DcPlan probe;
+    probe.build(n);
+    Layout L = layout_for(n, 64, nbq, probe.num_nodes(), probe.num_descs());
+    if (int rc = ensure_ws(c, L.total)) return rc;
+    c->dc = probe;
+    char* base = reinterpret_cast<char*>(c->ws);
+    char* p = base + L.tri + L.small;
+    double* dcws = reinterpret_cast<double*>(p); p += L.dc + L.fq;
+    DcNode* nodes = reinterpret_cast<DcNode*>(p); p += L.nodes;
+    DgemmDesc* descs = reinterpret_cast<DgemmDesc*>(p);
+    if (int rc = c->dc.upload(dcws, nodes, descs, c->st)) return rc;
+    c->dc_n = n;
+  }
+  Layout L = layout_for(n, 64, nbq, c->dc.num_nodes(), c->dc.num_descs());
+  char* base = reinterpret_cast<char*>(c->ws);
+  void* tri_ws = base;
+  double* sm = reinterpret_cast<double*>(base + L.tri);
+  double* d = sm; sm += n;
+  double* e = sm; sm += 4 * (size_t)n;
+  double* tau = sm; sm += n;
+  double* offd = sm; sm += n;
+  double* phi = sm; sm += 4 * (size_t)n;
+  double* lam = sm; sm += n;
+  void* fq_ws = base + L.tri + L.small + L.dc;
+  DgemmDesc* desc1 = reinterpret_cast<DgemmDesc*>(base + L.tri + L.small + L.dc + L.fq + L.nodes) + c->dc.num_descs();
+
+  // the solve runs on the context's streams, ordered after the caller's stream
+  ZQ_CUDA(cudaEventRecord(c->ev_fork, st));
+  ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
+
+  tm.mark("start", c->st);
+  TridiagView<double> v = tridiag_bind<double>(tri_ws, dD, n, ldd, 64, d, e, tau);
+  if (int rc = tridiagonalize<double>(v, nb, c->st)) return rc;
+  if (int rc = phase_reduce(e, n, offd, phi, c->st)) return rc;
+  tm.mark("tridiag", c->st);
+
+  if (vectors) {
+    // Q Phi on the second stream, overlapping the tridiagonal solve
+    ZQ_CUDA(cudaEventRecord(c->ev_fork, c->st));
+    ZQ_CUDA(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
+    double2* X = dD + (int64_t)n * ldd;  // right half as workspace (as the reference does)
+    if (int rc = form_q(dD, ldd, n, phi, X, ldd, nbq, fq_ws, c->st2)) return rc;
+    ZQ_CUDA(cudaEventRecord(c->ev_join, c->st2));
+    double* Z = nullptr;
+    if (int rc = c->dc.run(d, offd, lam, Z, c->st)) return rc;
+    tm.mark("stedc", c->st);
+    ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_join, 0));
+    tm.mark("formq-wait", c->st);
+    if (int rc = apply_z(X, ldd, Z, n, n, dD, ldd, desc1, c->st)) return rc;
+    tm.mark("apply_z", c->st);
+    if (int rc = symmetry_fill(dD, ldd, n, c->st)) return rc;
+    tm.mark("symfill", c->st);
+  } else {
+    double* Z = nullptr;
+    if (int rc = c->dc.run(d, offd, lam, Z, c->st)) return rc;
+  }
+  ZQ_CUDA(cudaMemcpyAsync(deig, lam, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->st));
+  ZQ_CUDA(cudaEventRecord(c->ev_join, c->st));
+  ZQ_CUDA(cudaStreamWaitEvent(st, c->ev_join, 0));
+  return ZQ_OK;
+}
+
+static int check_args(int n2, const void* D, int ld2, const void* eig) {
+  if (n2 < 0 || (n2 & 1)) { set_msg("n2 must be even and non-negative"); return ZQ_ERR_N2; }
+  if (n2 == 0) return ZQ_OK;
+  if (!D) { set_msg("D is null"); return ZQ_ERR_D; }
+  if (ld2 < n2) { set_msg("ld2 < n2"); return ZQ_ERR_LD; }
+  if (!eig) { set_msg("eig is null"); return ZQ_ERR_EIG; }
+  return ZQ_OK;
+}
+
+// host-memory drop-in
+static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors) {
+  if (int rc = check_args(n2, D, ld2, eig)) return rc;
+  if (n2 == 0) return ZQ_OK;
+  const int n = n2 / 2;
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  // device copy of D: n2 x n2 with ld = n2 (plus eigenvalues)
+  const size_t dbytes = sizeof(double2) * (size_t)n2 * n2;
+  double2* dD = nullptr;
+  double* deig = nullptr;
+  ZQ_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dD), dbytes + sizeof(double) * n + 256, c->st));
+  deig = reinterpret_cast<double*>(reinterpret_cast<char*>(dD) + dbytes);
+  int rc = ZQ_OK;
+  do {
+    // H1: only the left half is read
+    if (cudaMemcpy2DAsync(dD, sizeof(double2) * n2, D, sizeof(double2) * (size_t)ld2, sizeof(double2) * n2, n,
+                          cudaMemcpyHostToDevice, c->st) != cudaSuccess) { rc = ZQ_ERR_CUDA; set_msg("H2D copy failed"); break; }
+    rc = solve_device(c, dD, n2, n, deig, vectors, c->st);
+    if (rc) break;
+    if (vectors) {
+      if (cudaMemcpy2DAsync(D, sizeof(double2) * (size_t)ld2, dD, sizeof(double2) * n2, sizeof(double2) * n2, n2,
+                            cudaMemcpyDeviceToHost, c->st) != cudaSuccess) { rc = ZQ_ERR_CUDA; set_msg("D2H copy failed"); break; }
+    }
+    if (cudaMemcpyAsync(eig, deig, sizeof(double) * n, cudaMemcpyDeviceToHost, c->st) != cudaSuccess) {
+      rc = ZQ_ERR_CUDA; set_msg("D2H eig copy failed"); break;
+    }
+    cudaError_t e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) { set_last_error(e, "cudaStreamSynchronize", __FILE__, __LINE__); rc = ZQ_ERR_CUDA; break; }
+  } while (0);
+  cudaFreeAsync(dD, c->st);
+  cudaStreamSynchronize(c->st);
+  return rc;
+}
+
+// Batched: every matrix solved on the device through the per-matrix path.
+static int batched_solve(int count, const int* n2s, const int* ld2s, const long long* offs, const long long* eoffs,
+                         double2* dD, double* deig, cudaStream_t st) {
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  for (int b = 0; b < count; ++b) {
+    if (n2s[b] == 0) continue;
+    if (int rc = solve_device(c, dD + offs[b], ld2s[b], n2s[b] / 2, deig + eoffs[b], true, st)) return rc;
+  }
+  return ZQ_OK;
+}
+
+}  // namespace zq
+
+using namespace zq;
+
+extern "C" {
+
+int zquatev_c(int n2, double* D, int ld2, double* eig) {
+  return zquatev_host(n2, reinterpret_cast<double2*>(D), ld2, eig, true);
+}
+
+int zquatev_values(int n2, double* D, int ld2, double* eig) {
+  return zquatev_host(n2, reinterpret_cast<double2*>(D), ld2, eig, false);
+}
+
+int zquatev_device(int n2, double* dD, int ld2, double* deig, void* stream) {
+  if (int rc = check_args(n2, dD, ld2, deig)) return rc;
+  if (n2 == 0) return ZQ_OK;
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  return solve_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, true, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zquatev_values_device(int n2, double* dD, int ld2, double* deig, void* stream) {
+  if (int rc = check_args(n2, dD, ld2, deig)) return rc;
+  if (n2 == 0) return ZQ_OK;
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  return solve_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, false, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zq_stedc_device(int n, const double* d, const double* e, double* lam, double* Z, int ldz, void* stream) {
+  if (n < 0) { set_msg("n < 0"); return ZQ_ERR_ARG; }
+  if (n == 0) return ZQ_OK;
+  if (!d || !lam || !Z || (n > 1 && !e) || ldz < n) { set_msg("bad stedc arguments"); return ZQ_ERR_ARG; }
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (c->dc_n != n) {
+    DcPlan probe;
+    probe.build(n);
+    Layout L = layout_for(n, 64, g_nbq, probe.num_nodes(), probe.num_descs());
+    if (int rc = ensure_ws(c, L.total)) return rc;
+    c->dc = probe;
+    char* base = reinterpret_cast<char*>(c->ws);
+    char* p = base + L.tri + L.small;
+    double* dcws = reinterpret_cast<double*>(p); p += L.dc + L.fq;
+    DcNode* nodes = reinterpret_cast<DcNode*>(p); p += L.nodes;
+    if (int rc = c->dc.upload(dcws, nodes, reinterpret_cast<DgemmDesc*>(p), c->st)) return rc;
+    c->dc_n = n;
+  }
+  ZQ_CUDA(cudaEventRecord(c->ev_fork, st));
+  ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
+  double* Zi = nullptr;
+  if (int rc = c->dc.run(d, e, lam, Zi, c->st)) return rc;
+  ZQ_CUDA(cudaMemcpy2DAsync(Z, sizeof(double) * (size_t)ldz, Zi, sizeof(double) * n, sizeof(double) * n, n,
+                            cudaMemcpyDeviceToDevice, c->st));
+  ZQ_CUDA(cudaEventRecord(c->ev_join, c->st));
+  ZQ_CUDA(cudaStreamWaitEvent(st, c->ev_join, 0));
+  return ZQ_OK;
+}
+
+int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const long long* offs,
+                           const long long* eoffs, double* dD, double* deig, void* stream) {
+  if (count < 0 || (count > 0 && (!n2s || !ld2s || !offs || !eoffs || !dD || !deig))) {
+    set_msg("bad batched arguments");
+    return ZQ_ERR_ARG;
+  }
+  for (int b = 0; b < count; ++b)
+    if (int rc = check_args(n2s[b], dD, ld2s[b], deig)) return rc;
+  if (count == 0) return ZQ_OK;
+  return batched_solve(count, n2s, ld2s, offs, eoffs, reinterpret_cast<double2*>(dD), deig,
+                       reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zq_set_block_size(int nb) {
+  if (nb < 1 || nb > 64) { set_msg("block size must be in [1, 64]"); return ZQ_ERR_ARG; }
+  g_nb = nb;
+  return ZQ_OK;
+}
+
+int zq_get_block_size(void) { return g_nb; }
+
+const char* zq_last_error(void) { return last_error_message(); }
+
+int zq_version(void) { return 100; }
+
+int zq_release_workspace(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ZQ_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_ctx_mu);
+  Context* c = g_ctx[dev];
+  if (!c) return ZQ_OK;
+  std::lock_guard<std::mutex> lk2(c->mu);
+  cudaStreamSynchronize(c->st);
+  cudaStreamSynchronize(c->st2);
+  if (c->ws) cudaFree(c->ws);
+  c->ws = nullptr;
+  c->ws_bytes = 0;
+  c->dc_n = -1;
+  return ZQ_OK;
+}
+
+}  // extern "C"
+
+// The reference's own symbol (C++ linkage): ts::zquatev(int, std::complex<double>*, int, double*)
+namespace ts {
+int zquatev(const int n2, std::complex<double>* const D, const int ld2, double* const eig) {
+  return zquatev_c(n2, reinterpret_cast<double*>(D), ld2, eig);
+}
+}  // namespace ts

@@ -1,0 +1,225 @@
+// Back-transformation and output assembly.
+//
+// Reference: zquatev.cc:74-98 -- band extraction + zhbev, U = Q0 Z and
+// V = Q1 Z by zgemm3m (zquatev.cc:86-90), the explicit Q0/Q1 accumulated
+// during the panels (blocked.cc:477-544), and the symmetry fill of the right
+// half (zquatev.cc:92-98).
+//
+// Here Q is never accumulated during the reduction. After the tridiagonal is
+// known:
+//   1. phase_reduce: the quaternion subdiagonal e_k is made real by unit
+//      quaternions phi with phi_{k+1} = e_k phi_k / |e_k|, so that
+//      phi_{k+1}^H e_k phi_k = |e_k| (exact similarity, FP64);
+//   2. form_q: X = Q * [diag(alpha); diag(beta)] (the left half of Q Phi) by
+//      applying the stored reflectors backwards in compact-WY blocks,
+//      Q_blk = I - V T V^H, with the structured 2x2-block T built from the
+//      Gram matrix of the block's reflectors. Only the trailing (L x L)
+//      sub-blocks that can be non-zero are touched (zungtr-style);
+//   3. apply_z: (U; V) = X Z with the REAL eigenvector matrix Z of the
+//      real tridiagonal; complex X is read as a real array with twice the
+//      rows, so this is one real DGEMM;
+//   4. symmetry_fill: D[:, n:] = (-conj(V); conj(U)).
+#include "zq_common.cuh"
+#include "zq_kernels.h"
+
+namespace zq {
+
+// single thread: sequential quaternion products (n scalar steps)
+__global__ void k_phase(const double* e, int n, double* offd, double* phi) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double a0 = 1.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;  // phi_0 = 1
+  phi[0] = a0; phi[1] = a1; phi[2] = b0; phi[3] = b1;
+  for (int k = 0; k + 1 < n; ++k) {
+    const double ea0 = e[4 * k], ea1 = e[4 * k + 1], eb0 = e[4 * k + 2], eb1 = e[4 * k + 3];
+    const double nrm = sqrt(ea0 * ea0 + ea1 * ea1 + eb0 * eb0 + eb1 * eb1);
+    offd[k] = nrm;
+    if (nrm > 0.0) {
+      // q(ea, eb) * q(alpha, beta) = q(ea alpha - conj(eb) beta, eb alpha + conj(ea) beta)
+      double na0 = (ea0 * a0 - ea1 * a1) - (eb0 * b0 + eb1 * b1);
+      double na1 = (ea0 * a1 + ea1 * a0) - (eb0 * b1 - eb1 * b0);
+      double nb0 = (eb0 * a0 - eb1 * a1) + (ea0 * b0 + ea1 * b1);
+      double nb1 = (eb0 * a1 + eb1 * a0) + (ea0 * b1 - ea1 * b0);
+      const double s = 1.0 / sqrt(na0 * na0 + na1 * na1 + nb0 * nb0 + nb1 * nb1);
+      a0 = na0 * s; a1 = na1 * s; b0 = nb0 * s; b1 = nb1 * s;
+    } else {
+      a0 = 1.0; a1 = 0.0; b0 = 0.0; b1 = 0.0;
+    }
+    phi[4 * (k + 1) + 0] = a0; phi[4 * (k + 1) + 1] = a1;
+    phi[4 * (k + 1) + 2] = b0; phi[4 * (k + 1) + 3] = b1;
+  }
+}
+
+int phase_reduce(const double* e, int n, double* offd, double* phi, cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  k_phase<<<1, 32, 0, st>>>(e, n, offd, phi);
+  ZQ_LAUNCH_CHECK();
+  return ZQ_OK;
+}
+
+// X = [diag(alpha); diag(beta)]
+__global__ void k_init_x(double2* X, int64_t ldx, int n, const double* phi) {
+  const int64_t total = (int64_t)2 * n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t % (2 * n));
+    const int c = (int)(t / (2 * n));
+    double2 v = make_double2(0.0, 0.0);
+    if (r == c) v = make_double2(phi[4 * c], phi[4 * c + 1]);
+    else if (r == n + c) v = make_double2(phi[4 * c + 2], phi[4 * c + 3]);
+    X[r + (int64_t)c * ldx] = v;
+  }
+}
+
+// pack the block's reflectors: Wa[r, i] = A(p+1+r, p+i) for r >= i, else 0 (same for B)
+__global__ void k_pack_w(const double2* M, int64_t ldm, int n, int p, int kb, int L, double2* Wa, double2* Wb) {
+  const int64_t total = (int64_t)L * kb;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t % L), i = (int)(t / L);
+    double2 va = make_double2(0.0, 0.0), vb = va;
+    if (r >= i) {
+      const int64_t o = (p + 1 + r) + (int64_t)(p + i) * ldm;
+      va = M[o];
+      vb = M[n + o];
+    }
+    Wa[r + (int64_t)i * L] = va;
+    Wb[r + (int64_t)i * L] = vb;
+  }
+}
+
+// T (kb x kb quaternion, upper triangular) from G1 = <w_i, w_l>, G2 = [w_i, w_l]:
+//   T[k][k] = 1,  T[i][k] = - sum_{l<k} T[i][l] q(G1[l][k], G2[l][k])
+__global__ void k_build_t(const double2* G1, const double2* G2, int kb, double2* Ta, double2* Tb) {
+  const int i = threadIdx.x;
+  for (int t = i; t < kb * kb; t += blockDim.x) { Ta[t] = make_double2(0.0, 0.0); Tb[t] = make_double2(0.0, 0.0); }
+  __syncthreads();
+  for (int k = 0; k < kb; ++k) {
+    if (i < k) {
+      double2 sa = make_double2(0.0, 0.0), sb = sa;
+      for (int l = i; l < k; ++l) {
+        const double2 ta = Ta[i + l * kb], tb = Tb[i + l * kb];
+        const double2 g1 = G1[l + k * kb], g2 = G2[l + k * kb];
+        // q(ta, tb) q(g1, g2) = q(ta g1 - conj(tb) g2, tb g1 + conj(ta) g2)
+        cfma(sa, ta, g1); cfmac(sa, cneg(tb), g2);
+        cfma(sb, tb, g1); cfmac(sb, ta, g2);
+      }
+      Ta[i + k * kb] = cneg(sa);
+      Tb[i + k * kb] = cneg(sb);
+    }
+    if (i == k) { Ta[k + k * kb] = make_double2(1.0, 0.0); Tb[k + k * kb] = make_double2(0.0, 0.0); }
+    __syncthreads();
+  }
+}
+
+size_t form_q_workspace_bytes(int n, int nbq) {
+  // Wa, Wb (n x nbq), G1, G2, Ta, Tb (nbq^2), C1e, C1o, C2e, C2o (nbq x n)
+  return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n) + 256;
+}
+
+int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, int64_t ldx, int nbq, void* ws,
+           cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  k_init_x<<<ceil_div(2 * n * n, 256) > 4096 ? 4096 : ceil_div(2 * n * n, 256), 256, 0, st>>>(X, ldx, n, phi);
+  ZQ_LAUNCH_CHECK();
+  const int nref = n - 2;  // reflectors exist for columns 0..n-3
+  if (nref <= 0) return ZQ_OK;
+  double2* p = reinterpret_cast<double2*>(ws);
+  double2* Wa = p; p += (size_t)n * nbq;
+  double2* Wb = p; p += (size_t)n * nbq;
+  double2* G1 = p; p += (size_t)nbq * nbq;
+  double2* G2 = p; p += (size_t)nbq * nbq;
+  double2* Ta = p; p += (size_t)nbq * nbq;
+  double2* Tb = p; p += (size_t)nbq * nbq;
+  double2* C1e = p; p += (size_t)nbq * n;
+  double2* C1o = p; p += (size_t)nbq * n;
+  double2* C2e = p; p += (size_t)nbq * n;
+  double2* C2o = p;
+  double2* Xa = X;
+  double2* Xb = X + n;
+  const int nblocks = ceil_div(nref, nbq);
+  for (int bi = nblocks - 1; bi >= 0; --bi) {
+    const int pb = bi * nbq;
+    const int kb = (nbq < nref - pb) ? nbq : (nref - pb);
+    const int L = n - 1 - pb;
+    k_pack_w<<<ceil_div(L * kb, 256) > 2048 ? 2048 : ceil_div(L * kb, 256), 256, 0, st>>>(M, ldm, n, pb, kb, L, Wa, Wb);
+    ZQ_LAUNCH_CHECK();
+    ZgemmArgs g{};
+    // G1 = Wa^H Wa + Wb^H Wb ; G2 = Wa^T Wb - Wb^T Wa   (kb x kb, inner L)
+    g = ZgemmArgs{};
+    g.m = kb; g.n = kb; g.k1 = L; g.k2 = L;
+    g.A1 = Wa; g.lda1 = L; g.B1 = Wa; g.ldb1 = L;
+    g.A2 = Wb; g.lda2 = L; g.B2 = Wb; g.ldb2 = L;
+    g.s2 = 1.0; g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+    g.C = G1; g.ldc = kb;
+    if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
+    g.A1 = Wa; g.B1 = Wb; g.A2 = Wb; g.B2 = Wa; g.s2 = -1.0; g.C = G2;
+    if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
+    k_build_t<<<1, 64, 0, st>>>(G1, G2, kb, Ta, Tb);
+    ZQ_LAUNCH_CHECK();
+    // C1e = Wa^H Xa_sub + Wb^H Xb_sub ; C1o = Wa^T Xb_sub - Wb^T Xa_sub   (kb x L)
+    double2* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
+    double2* Xbs = Xb + (pb + 1) + (int64_t)(pb + 1) * ldx;
+    g = ZgemmArgs{};
+    g.m = kb; g.n = L; g.k1 = L; g.k2 = L;
+    g.A1 = Wa; g.lda1 = L; g.B1 = Xas; g.ldb1 = ldx;
+    g.A2 = Wb; g.lda2 = L; g.B2 = Xbs; g.ldb2 = ldx;
+    g.s2 = 1.0; g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+    g.C = C1e; g.ldc = kb;
+    if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
+    g.A1 = Wa; g.B1 = Xbs; g.A2 = Wb; g.B2 = Xas; g.s2 = -1.0; g.C = C1o;
+    if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
+    // C2e = Ta C1e - conj(Tb) C1o ; C2o = Tb C1e + conj(Ta) C1o   (kb x L)
+    g = ZgemmArgs{};
+    g.m = kb; g.n = L; g.k1 = kb; g.k2 = kb;
+    g.A1 = Ta; g.lda1 = kb; g.B1 = C1e; g.ldb1 = kb;
+    g.A2 = Tb; g.lda2 = kb; g.B2 = C1o; g.ldb2 = kb;
+    g.s2 = -1.0; g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+    g.C = C2e; g.ldc = kb;
+    if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
+    g.A1 = Tb; g.A2 = Ta; g.s2 = 1.0; g.C = C2o;
+    if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
+    // Xa_sub -= Wa C2e - conj(Wb) C2o ; Xb_sub -= Wb C2e + conj(Wa) C2o   (L x L)
+    g = ZgemmArgs{};
+    g.m = L; g.n = L; g.k1 = kb; g.k2 = kb;
+    g.A1 = Wa; g.lda1 = L; g.B1 = C2e; g.ldb1 = kb;
+    g.A2 = Wb; g.lda2 = L; g.B2 = C2o; g.ldb2 = kb;
+    g.s2 = -1.0; g.alpha = make_double2(-1.0, 0.0); g.beta = make_double2(1.0, 0.0);
+    g.C = Xas; g.ldc = ldx;
+    if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
+    g.A1 = Wb; g.A2 = Wa; g.s2 = 1.0; g.C = Xbs;
+    if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
+  }
+  return ZQ_OK;
+}
+
+int apply_z(const double2* X, int64_t ldx, const double* Z, int64_t ldz, int n, double2* out, int64_t ldo,
+            DgemmDesc* dev_desc, cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  DgemmDesc d{};
+  d.A = reinterpret_cast<const double*>(X); d.lda = 2 * ldx;
+  d.B = Z; d.ldb = ldz;
+  d.C = reinterpret_cast<double*>(out); d.ldc = 2 * ldo;
+  d.m = 4 * n; d.n = n; d.k = n;
+  d.alpha = 1.0; d.beta = 0.0;
+  return dgemm_grouped(&d, 1, dev_desc, st);
+}
+
+__global__ void k_symfill(double2* D, int64_t ld, int n) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t % n), i = (int)(t / n);
+    const double2 u = D[j + (int64_t)i * ld];
+    const double2 v = D[n + j + (int64_t)i * ld];
+    D[j + (int64_t)(n + i) * ld] = make_double2(-v.x, v.y);      // -conj(V)
+    D[n + j + (int64_t)(n + i) * ld] = make_double2(u.x, -u.y);  // conj(U)
+  }
+}
+
+int symmetry_fill(double2* D, int64_t ld, int n, cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  const int64_t total = (int64_t)n * n;
+  const int blocks = (int)((total + 255) / 256 > 8192 ? 8192 : (total + 255) / 256);
+  k_symfill<<<blocks, 256, 0, st>>>(D, ld, n);
+  ZQ_LAUNCH_CHECK();
+  return ZQ_OK;
+}
+
+}  // namespace zq

@@ -1,0 +1,129 @@
+// Shared device/host helpers for the GB300 quaternion eigensolver.
+//
+// Storage convention used by every kernel: a quaternion-Hermitian matrix
+// H = (A -B*; B A*) is held as its left half [A; B] -- a 2n x n complex,
+// column-major array with leading dimension ld (A at rows 0..n-1, B at rows
+// n..2n-1), exactly the part of the caller's array the reference reads
+// (zquatev.cc:47-54). A quaternion vector u is the pair (ua, ub) of complex
+// n-vectors; its partner column J*conj(u) = (-conj(ub), conj(ua)) is implied.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+namespace zq {
+
+// ----------------------------------------------------------------------------
+// complex helpers (double2 / float2)
+// ----------------------------------------------------------------------------
+template <typename R> struct cplx_of;
+template <> struct cplx_of<double> { using type = double2; };
+template <> struct cplx_of<float> { using type = float2; };
+template <typename R> using cplx = typename cplx_of<R>::type;
+
+__host__ __device__ __forceinline__ double2 mk(double x, double y) { return make_double2(x, y); }
+__host__ __device__ __forceinline__ float2 mk(float x, float y) { return make_float2(x, y); }
+
+template <typename Z> __host__ __device__ __forceinline__ Z cadd(Z a, Z b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename Z> __host__ __device__ __forceinline__ Z csub(Z a, Z b) { return mk(a.x - b.x, a.y - b.y); }
+template <typename Z> __host__ __device__ __forceinline__ Z cneg(Z a) { return mk(-a.x, -a.y); }
+template <typename Z> __host__ __device__ __forceinline__ Z cconj(Z a) { return mk(a.x, -a.y); }
+template <typename Z> __host__ __device__ __forceinline__ Z cmul(Z a, Z b) {
+  return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) * b
+template <typename Z> __host__ __device__ __forceinline__ Z cmulc(Z a, Z b) {
+  return mk(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+template <typename Z, typename R> __host__ __device__ __forceinline__ Z cscale(Z a, R s) { return mk(a.x * s, a.y * s); }
+template <typename Z> __host__ __device__ __forceinline__ auto cabs2(Z a) -> decltype(a.x) { return a.x * a.x + a.y * a.y; }
+// acc += a * b
+template <typename Z> __host__ __device__ __forceinline__ void cfma(Z& acc, Z a, Z b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename Z> __host__ __device__ __forceinline__ void cfmac(Z& acc, Z a, Z b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y); acc.y = fma(-a.y, b.x, acc.y);
+}
+// acc += a * conj(b)
+template <typename Z> __host__ __device__ __forceinline__ void cfmacb(Z& acc, Z a, Z b) {
+  acc.x = fma(a.x, b.x, acc.x); acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.y, b.x, acc.y); acc.y = fma(-a.x, b.y, acc.y);
+}
+
+template <typename Z> __host__ __device__ __forceinline__ Z czero() { Z z; z.x = 0; z.y = 0; return z; }
+
+// ----------------------------------------------------------------------------
+// block reductions
+// ----------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+template <typename T> __device__ __forceinline__ T warp_max(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+// Sum over the block; every thread gets the result. `sh` needs blockDim/32 slots.
+template <typename T> __device__ T block_sum(T v, T* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T r = 0;
+  for (int i = 0; i < nw; ++i) r += sh[i];
+  return r;
+}
+template <typename T> __device__ T block_max(T v, T* sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T r = sh[0];
+  for (int i = 1; i < nw; ++i) r = fmax(r, sh[i]);
+  return r;
+}
+
+// ----------------------------------------------------------------------------
+// error handling (host)
+// ----------------------------------------------------------------------------
+// Status codes returned through the C ABI. Positive values are the
+// tridiagonal solver's non-convergence count, as LAPACK's info (zquatev.cc:99).
+enum Status : int {
+  ZQ_OK = 0,
+  ZQ_ERR_N2 = -1,       // n2 negative or odd (the reference asserts n2 % 2 == 0, zquatev.cc:43)
+  ZQ_ERR_D = -2,        // null D with n2 > 0
+  ZQ_ERR_LD = -3,       // ld2 < max(1, n2)
+  ZQ_ERR_EIG = -4,      // null eig with n2 > 0
+  ZQ_ERR_ARG = -5,      // other invalid argument
+  ZQ_ERR_CUDA = -100,   // a CUDA runtime call failed
+  ZQ_ERR_NOMEM = -101,  // device allocation failed
+  ZQ_ERR_NOTFINITE = -102,  // input contains Inf/NaN
+  ZQ_ERR_LIMIT = -103,  // size above a fixed limit of the called entry point
+};
+
+#define ZQ_CUDA(call)                                                        \
+  do {                                                                       \
+    cudaError_t _e = (call);                                                 \
+    if (_e != cudaSuccess) {                                                 \
+      zq::set_last_error(_e, #call, __FILE__, __LINE__);                     \
+      return (_e == cudaErrorMemoryAllocation) ? zq::ZQ_ERR_NOMEM : zq::ZQ_ERR_CUDA; \
+    }                                                                        \
+  } while (0)
+
+#define ZQ_LAUNCH_CHECK() ZQ_CUDA(cudaGetLastError())
+
+void set_last_error(cudaError_t e, const char* what, const char* file, int line);
+const char* last_error_message();
+
+inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace zq

@@ -1,0 +1,247 @@
+// Stage (b) GEMMs: FP64 complex (Gauss 3M) and real matrix products.
+//
+// The reference forms these products with zgemm3m (blocked.cc:424-543,
+// zquatev.cc:87-90). On GB300 the FP64 tensor path (DMMA, mma.sync .f64) issues
+// slower than plain DFMA (1.05 vs 1.19 TFLOP/s measured), so the FP64 products
+// are register-tiled DFMA kernels: 64x64 output tile per CTA, 256 threads, a
+// 4x4 micro-tile per thread, operands staged through shared memory.
+//
+// zgemm computes  C = alpha * (opA1(A1) opB1(B1) + s2 * opA2(A2) opB2(B2)) + beta * C
+// with op in {N, T, C (conj-transpose), R (conj, no transpose)} chosen per
+// operand at compile time; the complex products use the 3M (Gauss) scheme:
+//   T1 = Ar Br, T2 = Ai Bi, T3 = (Ar + Ai)(Br + Bi); Re = T1 - T2, Im = T3 - T1 - T2,
+// i.e. 3 real multiply-adds per complex multiply-add (the reference's zgemm3m).
+//
+// dgemm_grouped computes a list of independent real products
+//   C_g = alpha_g op(A_g) op(B_g) + beta_g C_g
+// in one launch (flat tile index over the group), used by the back-transform
+// (G Z with complex G viewed as a real array of twice the rows) and by the
+// divide-and-conquer merges.
+#include "zq_common.cuh"
+#include "zq_kernels.h"
+
+namespace zq {
+
+constexpr int GT = 64;   // output tile edge
+constexpr int GK = 8;    // k per stage (complex)
+constexpr int GKR = 16;  // k per stage (real)
+constexpr int GNT = 256;
+
+template <int OP>
+__device__ __forceinline__ double2 load_op(const double2* X, int64_t ldx, int r, int c) {
+  // element (r, c) of op(X)
+  if (OP == OP_N) return X[r + (int64_t)c * ldx];
+  if (OP == OP_R) { double2 v = X[r + (int64_t)c * ldx]; v.y = -v.y; return v; }
+  if (OP == OP_T) return X[c + (int64_t)r * ldx];
+  double2 v = X[c + (int64_t)r * ldx]; v.y = -v.y; return v;  // OP_C
+}
+
+template <int OPA1, int OPB1, int OPA2, int OPB2>
+__global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
+  __shared__ double sA[3][GK][GT];
+  __shared__ double sB[3][GK][GT];
+  const int tid = threadIdx.x;
+  const int tr = tid & 15, tc = tid >> 4;
+  const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
+  const int bz = blockIdx.z;
+  const double2* A1 = g.A1 + bz * g.sA1;
+  const double2* B1 = g.B1 + bz * g.sB1;
+  const double2* A2 = g.A2 ? g.A2 + bz * g.sA2 : nullptr;
+  const double2* B2 = g.B2 ? g.B2 + bz * g.sB2 : nullptr;
+  double2* C = g.C + bz * g.sC;
+  double t1[4][4], t2[4][4], t3[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) { t1[a][b] = 0.0; t2[a][b] = 0.0; t3[a][b] = 0.0; }
+
+  const int nseg = (A2 != nullptr) ? 2 : 1;
+  for (int seg = 0; seg < nseg; ++seg) {
+    const int K = seg == 0 ? g.k1 : g.k2;
+    const double sgn = seg == 0 ? 1.0 : g.s2;
+    for (int k0 = 0; k0 < K; k0 += GK) {
+      __syncthreads();
+      for (int e = tid; e < GK * GT; e += GNT) {
+        // A tile: 64 rows x GK; B tile: GK x 64 cols
+        int r, kk;
+        const bool a_kfast = (seg == 0 ? (OPA1 == OP_T || OPA1 == OP_C) : (OPA2 == OP_T || OPA2 == OP_C));
+        if (a_kfast) { kk = e % GK; r = e / GK; } else { r = e % GT; kk = e / GT; }
+        double2 va = make_double2(0.0, 0.0);
+        if (i0 + r < g.m && k0 + kk < K) {
+          va = seg == 0 ? load_op<OPA1>(A1, g.lda1, i0 + r, k0 + kk) : load_op<OPA2>(A2, g.lda2, i0 + r, k0 + kk);
+          va.x *= sgn; va.y *= sgn;
+        }
+        sA[0][kk][r] = va.x; sA[1][kk][r] = va.y; sA[2][kk][r] = va.x + va.y;
+        int c;
+        const bool b_kfast = (seg == 0 ? (OPB1 == OP_N || OPB1 == OP_R) : (OPB2 == OP_N || OPB2 == OP_R));
+        if (b_kfast) { kk = e % GK; c = e / GK; } else { c = e % GT; kk = e / GT; }
+        double2 vb = make_double2(0.0, 0.0);
+        if (j0 + c < g.n && k0 + kk < K)
+          vb = seg == 0 ? load_op<OPB1>(B1, g.ldb1, k0 + kk, j0 + c) : load_op<OPB2>(B2, g.ldb2, k0 + kk, j0 + c);
+        sB[0][kk][c] = vb.x; sB[1][kk][c] = vb.y; sB[2][kk][c] = vb.x + vb.y;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < GK; ++kk) {
+        double ar[4], ai[4], as[4], br[4], bi[4], bs[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          ar[q] = sA[0][kk][tr + 16 * q]; ai[q] = sA[1][kk][tr + 16 * q]; as[q] = sA[2][kk][tr + 16 * q];
+          br[q] = sB[0][kk][tc + 16 * q]; bi[q] = sB[1][kk][tc + 16 * q]; bs[q] = sB[2][kk][tc + 16 * q];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+            t1[a][b] = fma(ar[a], br[b], t1[a][b]);
+            t2[a][b] = fma(ai[a], bi[b], t2[a][b]);
+            t3[a][b] = fma(as[a], bs[b], t3[a][b]);
+          }
+      }
+    }
+  }
+  const double2 al = g.alpha, be = g.beta;
+  const bool use_beta = (be.x != 0.0 || be.y != 0.0);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + tr + 16 * a;
+    if (i >= g.m) continue;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + tc + 16 * b;
+      if (j >= g.n) continue;
+      const double re = t1[a][b] - t2[a][b];
+      const double im = t3[a][b] - t1[a][b] - t2[a][b];
+      double2 out = make_double2(al.x * re - al.y * im, al.x * im + al.y * re);
+      const int64_t o = i + (int64_t)j * g.ldc;
+      if (use_beta) {
+        const double2 c = C[o];
+        out.x += be.x * c.x - be.y * c.y;
+        out.y += be.x * c.y + be.y * c.x;
+      }
+      C[o] = out;
+    }
+  }
+}
+
+template <int OPA1, int OPB1, int OPA2, int OPB2>
+int zgemm_launch(const ZgemmArgs& g, int batch, cudaStream_t st) {
+  if (g.m <= 0 || g.n <= 0) return ZQ_OK;
+  dim3 grid(ceil_div(g.m, GT), ceil_div(g.n, GT), batch);
+  k_zgemm<OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
+  ZQ_LAUNCH_CHECK();
+  return ZQ_OK;
+}
+
+int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, int batch, cudaStream_t st) {
+#define ZQ_Z(a, b, c, d) \
+  if (opa1 == a && opb1 == b && opa2 == c && opb2 == d) return zgemm_launch<a, b, c, d>(g, batch, st);
+  // the combinations used by the solver
+  ZQ_Z(OP_C, OP_N, OP_C, OP_N)   // Wa^H Xa + Wb^H Xb
+  ZQ_Z(OP_T, OP_N, OP_T, OP_N)   // Wa^T Xb - Wb^T Xa
+  ZQ_Z(OP_N, OP_N, OP_R, OP_N)   // Wa C - conj(Wb) D
+  ZQ_Z(OP_N, OP_N, OP_N, OP_N)
+  ZQ_Z(OP_C, OP_N, OP_N, OP_N)
+  ZQ_Z(OP_N, OP_C, OP_N, OP_N)
+  ZQ_Z(OP_T, OP_N, OP_N, OP_N)
+#undef ZQ_Z
+  return ZQ_ERR_ARG;
+}
+
+// ----------------------------------------------------------------------------
+// real grouped GEMM
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDesc* __restrict__ descs, int count) {
+  __shared__ double sA[GKR][GT];
+  __shared__ double sB[GKR][GT + 1];
+  // locate descriptor (linear search over prefix offsets; count is small)
+  const int t = blockIdx.x;
+  int gi = 0;
+  {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (descs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+    }
+    gi = lo;
+  }
+  const DgemmDesc d = descs[gi];
+  const int local = t - d.tile0;
+  const int mt = (d.m + GT - 1) / GT;
+  const int i0 = (local % mt) * GT, j0 = (local / mt) * GT;
+  const int tid = threadIdx.x;
+  const int tr = tid & 15, tc = tid >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+  for (int k0 = 0; k0 < d.k; k0 += GKR) {
+    __syncthreads();
+    for (int e = tid; e < GKR * GT; e += GNT) {
+      int r, kk;
+      if (d.ta) { kk = e % GKR; r = e / GKR; } else { r = e % GT; kk = e / GT; }
+      double va = 0.0;
+      if (i0 + r < d.m && k0 + kk < d.k)
+        va = d.ta ? d.A[(k0 + kk) + (int64_t)(i0 + r) * d.lda] : d.A[(i0 + r) + (int64_t)(k0 + kk) * d.lda];
+      sA[kk][r] = va;
+      int c;
+      if (!d.tb) { kk = e % GKR; c = e / GKR; } else { c = e % GT; kk = e / GT; }
+      double vb = 0.0;
+      if (j0 + c < d.n && k0 + kk < d.k)
+        vb = d.tb ? d.B[(j0 + c) + (int64_t)(k0 + kk) * d.ldb] : d.B[(k0 + kk) + (int64_t)(j0 + c) * d.ldb];
+      sB[kk][c] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GKR; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) { a[q] = sA[kk][tr + 16 * q]; b[q] = sB[kk][tc + 16 * q]; }
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) acc[x][y] = fma(a[x], b[y], acc[x][y]);
+    }
+  }
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    const int i = i0 + tr + 16 * x;
+    if (i >= d.m) continue;
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      const int j = j0 + tc + 16 * y;
+      if (j >= d.n) continue;
+      const int64_t o = i + (int64_t)j * d.ldc;
+      double out = d.alpha * acc[x][y];
+      if (d.beta != 0.0) out += d.beta * d.C[o];
+      d.C[o] = out;
+    }
+  }
+}
+
+void k_dgemm_grouped_launch(const DgemmDesc* dev_descs, int count, int tiles, cudaStream_t st) {
+  if (tiles <= 0 || count <= 0) return;
+  k_dgemm_grouped<<<tiles, GNT, 0, st>>>(dev_descs, count);
+}
+
+int dgemm_tiles(int m, int n) { return ceil_div(m, GT) * ceil_div(n, GT); }
+
+int dgemm_grouped(DgemmDesc* host_descs, int count, DgemmDesc* dev_descs, cudaStream_t st) {
+  int tiles = 0;
+  int used = 0;
+  for (int i = 0; i < count; ++i) {
+    DgemmDesc& d = host_descs[i];
+    if (d.m <= 0 || d.n <= 0) continue;
+    d.tile0 = tiles;
+    tiles += ceil_div(d.m, GT) * ceil_div(d.n, GT);
+    host_descs[used++] = d;
+  }
+  if (used == 0) return ZQ_OK;
+  ZQ_CUDA(cudaMemcpyAsync(dev_descs, host_descs, sizeof(DgemmDesc) * used, cudaMemcpyHostToDevice, st));
+  k_dgemm_grouped<<<tiles, GNT, 0, st>>>(dev_descs, used);
+  ZQ_LAUNCH_CHECK();
+  return ZQ_OK;
+}
+
+}  // namespace zq

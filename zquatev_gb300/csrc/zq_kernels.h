@@ -1,0 +1,121 @@
+// Internal interfaces between the solver's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <vector>
+
+#include "zq_common.cuh"
+
+namespace zq {
+
+// ---------------------------------------------------------------- tridiagonal
+template <typename R>
+struct TridiagView {
+  cplx<R>* M;      // [A; B], 2n x n, column-major
+  int n;
+  int64_t ld;
+  cplx<R>* Ya;     // panel aux vectors, n x nbmax (global row index), ld = ldy
+  cplx<R>* Yb;
+  int64_t ldy;
+  int nbmax;
+  cplx<R>* ga;     // g of the current column (n)
+  cplx<R>* gb;
+  cplx<R>* hpart;  // hemv tile partials: hblk x hblk x 64 x 4
+  int hblk;
+  cplx<R>* dpart;  // dot partials: hblk x nbmax x 4
+  cplx<R>* dots;   // 4 * nbmax
+  double* npart;   // norm partials: 2 * hblk
+  double* cpart;   // c partials: hblk
+  double* scal;    // per-column scalars (8)
+  double* d;       // diagonal (n)
+  double* e;       // quaternion subdiagonal (4 doubles each, n)
+  double* tau;     // 1 if reflector j exists else 0 (n)
+};
+
+template <typename R>
+size_t tridiag_workspace_bytes(int n, int nbmax);
+template <typename R>
+TridiagView<R> tridiag_bind(void* ws, cplx<R>* M, int n, int64_t ld, int nbmax, double* d, double* e, double* tau);
+template <typename R>
+int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st);
+
+// ---------------------------------------------------------------------- GEMM
+enum { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };
+
+struct ZgemmArgs {
+  int m, n, k1, k2;
+  const double2* A1; int64_t lda1; int64_t sA1;
+  const double2* B1; int64_t ldb1; int64_t sB1;
+  const double2* A2; int64_t lda2; int64_t sA2;
+  const double2* B2; int64_t ldb2; int64_t sB2;
+  double s2;
+  double2 alpha, beta;
+  double2* C; int64_t ldc; int64_t sC;
+};
+int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, int batch, cudaStream_t st);
+
+struct DgemmDesc {
+  const double* A; const double* B; double* C;
+  int64_t lda, ldb, ldc;
+  int64_t off_a, off_b, off_c;  // plan-time offsets (bound to pointers before upload)
+  int m, n, k;
+  int ta, tb;
+  int tile0;
+  double alpha, beta;
+};
+int dgemm_grouped(DgemmDesc* host_descs, int count, DgemmDesc* dev_descs, cudaStream_t st);
+void k_dgemm_grouped_launch(const DgemmDesc* dev_descs, int count, int tiles, cudaStream_t st);
+int dgemm_tiles(int m, int n);
+
+// ------------------------------------------------------------------ D&C (c)
+struct DcNode {
+  int a, c, b;
+  int K, ndefl, nrot;
+  double rho, rho2;
+};
+struct DcWork {
+  double *sd, *sz, *nd_val, *nd_z, *df_val, *df_sval, *rot_c, *rot_s, *r_tau, *r_lam, *zhat;
+  int *perm, *nd_col, *df_col, *df_scol, *rot_p, *rot_j, *r_orig;
+};
+struct DcPlan {
+  int n = 0;
+  int max_depth = 0;
+  std::vector<DcNode> nodes_host;
+  std::vector<int> depth_off, depth_cnt, leaf_off, leaf_cnt;
+  std::vector<DgemmDesc> gemm_host;
+  std::vector<int> gemm_off, gemm_tiles;
+  // device
+  double* base = nullptr;
+  double* Z[2] = {nullptr, nullptr};
+  double* Mb = nullptr;
+  double* lam[2] = {nullptr, nullptr};
+  double *dmod = nullptr, *es = nullptr, *scal = nullptr;
+  DcWork w{};
+  DcNode* nodes_dev = nullptr;
+  DgemmDesc* descs_dev = nullptr;
+
+  static size_t workspace_doubles(int n);
+  int build(int n);
+  size_t num_nodes() const { return nodes_host.size(); }
+  size_t num_descs() const { return gemm_host.size(); }
+  int upload(double* ws, DcNode* dnodes, DgemmDesc* ddescs, cudaStream_t st);
+  // d (n), e (n-1) on device; lam_out (n) on device; z_out points into the workspace
+  int run(const double* d, const double* e, double* lam_out, double*& z_out, cudaStream_t st);
+};
+
+// ------------------------------------------------------------ back-transform
+// phase reduction of the quaternion tridiagonal: e (4 doubles per entry) ->
+// real off-diagonal |e_k| and unit quaternions phi_k = (alpha_k, beta_k)
+int phase_reduce(const double* e, int n, double* offd, double* phi, cudaStream_t st);
+// X = [diag(alpha); diag(beta)] (2n x n complex, ld), then Q X by blocked reflectors
+int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, int64_t ldx,
+           int nbq, void* ws, cudaStream_t st);
+size_t form_q_workspace_bytes(int n, int nbq);
+// out (2n x n complex, ldo) = X (2n x n complex, ldx) * Z (n x n real, ldz)
+int apply_z(const double2* X, int64_t ldx, const double* Z, int64_t ldz, int n, double2* out, int64_t ldo,
+            DgemmDesc* dev_desc, cudaStream_t st);
+// right half of the n2 x n2 output from the left half (U; V)
+int symmetry_fill(double2* D, int64_t ld, int n, cudaStream_t st);
+
+}  // namespace zq

@@ -1,0 +1,72 @@
+"""Python mirror of the reference's public call, ts::zquatev (zquatev.h:54).
+
+``zquatev(n2, D, ld2, eig)`` has the reference's argument meaning and error
+behaviour: D is a column-major (ld2, n2) complex128 array whose left half holds
+[A; B]; it is overwritten with the eigenvectors in the (U -V*; V U*) layout;
+eig[:n] receives the ascending eigenvalues; the return value is the solver's
+info (0 on success). The work runs on the GPU through libzquatev_gb300.so.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+
+
+def _check_host(d: np.ndarray, eig: np.ndarray) -> None:
+    if d.dtype != np.complex128 or not d.flags.f_contiguous:
+        raise TypeError("D must be a Fortran-ordered complex128 array (column-major)")
+    if eig.dtype != np.float64 or not eig.flags.c_contiguous:
+        raise TypeError("eig must be a contiguous float64 array")
+
+
+def zquatev(n2: int, d: np.ndarray, ld2: int, eig: np.ndarray) -> int:
+    """In-place drop-in for ts::zquatev on host arrays; returns info."""
+    _check_host(d, eig)
+    if d.shape[0] != ld2 or (n2 and d.shape[1] < n2) or eig.size < n2 // 2:
+        raise ValueError("array shapes do not match n2 / ld2")
+    return _lib.load().zquatev_c(n2, d.ctypes.data, ld2, eig.ctypes.data)
+
+
+def eigvals(n2: int, d: np.ndarray, ld2: int, eig: np.ndarray) -> int:
+    """Eigenvalues only (D is used as scratch)."""
+    _check_host(d, eig)
+    return _lib.load().zquatev_values(n2, d.ctypes.data, ld2, eig.ctypes.data)
+
+
+def solve(d: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Convenience: returns (eigenvalues (n,), eigenvectors (n2, n2)) for a (ld2, n2) input."""
+    out = np.array(d, dtype=np.complex128, order="F", copy=True)
+    n2 = out.shape[1]
+    eig = np.zeros(max(n2, 1))
+    _lib.check(zquatev(n2, out, out.shape[0], eig), "zquatev_c")
+    return eig[: n2 // 2].copy(), out[:n2]
+
+
+# --------------------------------------------------------------- device (torch)
+def zquatev_device(dmat, deig, stream=None) -> int:
+    """Device-pointer variant on torch tensors.
+
+    dmat: complex128 CUDA tensor of shape (n2, ld2) holding D^T row-major, i.e.
+    the column-major (ld2, n2) array's memory; deig: float64 CUDA tensor (>= n).
+    Runs on ``stream`` (default: torch's current stream) without synchronising.
+    """
+    import torch
+
+    if dmat.dtype != torch.complex128 or not dmat.is_cuda or not dmat.is_contiguous():
+        raise TypeError("dmat must be a contiguous complex128 CUDA tensor")
+    n2, ld2 = dmat.shape[0], dmat.shape[1]
+    st = stream if stream is not None else torch.cuda.current_stream(dmat.device)
+    return _lib.load().zquatev_device(n2, dmat.data_ptr(), ld2, deig.data_ptr(), st.cuda_stream)
+
+
+def stedc_device(d, e, lam, z, stream=None) -> int:
+    """Real symmetric tridiagonal eigensolver on torch float64 CUDA tensors.
+
+    z is an (n, n) tensor receiving Z^T row-major (= Z column-major)."""
+    import torch
+
+    n = d.numel()
+    st = stream if stream is not None else torch.cuda.current_stream(d.device)
+    return _lib.load().zq_stedc_device(n, d.data_ptr(), e.data_ptr() if n > 1 else 0, lam.data_ptr(),
+                                       z.data_ptr(), n, st.cuda_stream)
