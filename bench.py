@@ -1,0 +1,404 @@
+"""Benchmark: quaternion-Hermitian eigensolve on GB300 (one JSON line on rank 0).
+
+Workload (default): one n2 = 8192 (n = 4096) random quaternion-Hermitian
+matrix, complex128, A = (X + X^H)/2, B = (Y - Y^T)/2, Re/Im ~ N(0,1), full
+eigenvectors -- the "plain FP64 GPU drop-in at scale" case. A step is one full
+solve of that matrix. Inputs (512 MiB left half) are larger than L2, so no
+extra L2 flush is needed between steps.
+
+  value   device-resident: the input is restored from an HBM master copy
+          (device-to-device) and solved through the device C ABI; ms per solve.
+  e2e     the reference-facing host call (zquatev_c on a host array): H2D of
+          the left half, solve, D2H of all of D and eig, per solve.
+  roofline  the dominant kernel class, timed with CUDA events on its launch
+          stream during the timed region, against the FP64 DFMA peak measured
+          here by a calibration kernel (the FP64 path does not use tensor
+          cores: DMMA issues slower than DFMA on this part).
+  cpu_baseline  the oracle (numpy/scipy restatement of the reference, the only
+          CPU implementation that exists on the GPU host) on a bounded n2=1024
+          sample, scaled by n^3 to n2 = 8192.
+
+--impl reference runs the CPU reference arm (oracle port, all host threads).
+Under torchrun (N > 1) every rank solves its own matrix (replicas, no
+collectives on the data path); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "n2=8192 solve ms; mixed-stream solves/s, p99 ms vs plain FP64 at resid≤1e-12"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n2", type=int, default=8192)
+    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--no-check", action="store_true")
+    p.add_argument("--cpu-sample-n2", type=int, default=1024)
+    return p.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# --------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- FP64 peak probe
+_PEAK_SRC = r"""
+extern "C" __global__ void dfma_peak(double* out, int iters, double a, double b) {
+  double x0=threadIdx.x, x1=x0+1, x2=x0+2, x3=x0+3, x4=x0+4, x5=x0+5, x6=x0+6, x7=x0+7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0,a,b); x1 = fma(x1,a,b); x2 = fma(x2,a,b); x3 = fma(x3,a,b);
+    x4 = fma(x4,a,b); x5 = fma(x5,a,b); x6 = fma(x6,a,b); x7 = fma(x7,a,b);
+  }
+  out[blockIdx.x*blockDim.x+threadIdx.x] = x0+x1+x2+x3+x4+x5+x6+x7;
+}
+"""
+
+
+def fp64_peak_tflops() -> float:
+    """DFMA throughput of this GPU (TFLOP/s), timed with CUDA events."""
+    import torch
+
+    lib = _peak_module()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 4, 256, 4096
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.run(out, blocks, threads, iters)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, 2.0 * 8 * iters * blocks * threads / (ms * 1e9))
+    return best
+
+
+_PEAK_LIB = None
+
+
+def _peak_module():
+    """Compiles the calibration kernel with nvcc into a tiny shared library."""
+    global _PEAK_LIB
+    if _PEAK_LIB is not None:
+        return _PEAK_LIB
+    import ctypes
+    import tempfile
+
+    import torch
+
+    d = tempfile.mkdtemp(prefix="zqpeak")
+    src = os.path.join(d, "peak.cu")
+    with open(src, "w") as f:
+        f.write(_PEAK_SRC + r"""
+extern "C" int launch_peak(double* out, int blocks, int threads, int iters, void* st) {
+  dfma_peak<<<blocks, threads, 0, (cudaStream_t)st>>>(out, iters, 0.999, 1e-3);
+  return (int)cudaGetLastError();
+}
+""")
+    so = os.path.join(d, "peak.so")
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-shared", "-Xcompiler", "-fPIC",
+                    "-cudart", "shared", src, "-o", so], check=True, capture_output=True)
+    lib = ctypes.CDLL(so)
+    lib.launch_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+
+    class _M:
+        @staticmethod
+        def run(out, blocks, threads, iters):
+            lib.launch_peak(out.data_ptr(), blocks, threads, iters, torch.cuda.current_stream().cuda_stream)
+
+    _PEAK_LIB = _M
+    return _M
+
+
+# ------------------------------------------------------------------ CPU legs
+def cpu_sample(n2_sample: int, n2_target: int, threads: int):
+    """Times the oracle (numpy/scipy restatement of the reference) on one
+    n2_sample solve and scales by n^3 to n2_target."""
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", str(threads))
+    from oracle import port
+    from zquatev_gb300 import inputs
+
+    n = n2_sample // 2
+    d = inputs.random_matrix(n, 4321)
+    eig = np.zeros(2 * n)
+    t0 = time.perf_counter()
+    rc = port.zquatev(2 * n, d, 2 * n, eig)
+    dt = time.perf_counter() - t0
+    assert rc == 0
+    scale = (n2_target / n2_sample) ** 3
+    return dt * 1e3 * scale, dt
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ["OPENBLAS_NUM_THREADS"] = str(threads)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        ms, raw = cpu_sample(args.cpu_sample_n2, args.n2, threads)
+        if i >= args.warmup:
+            vals.append(ms)
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": f"single quaternion-Hermitian solve n2={args.n2} (random, complex128), "
+                               f"timed as n2={args.cpu_sample_n2} samples scaled by n^3"},
+        "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": f"one n2={args.cpu_sample_n2} solve per step through oracle/port.py "
+                                   f"(numpy + scipy OpenBLAS/LAPACK), x{(args.n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
+        "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- GPU arm
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from zquatev_gb300 import _lib, build, inputs, metrics, solver
+
+    if not build.up_to_date():
+        build.build()
+    lib = _lib.load()
+    n2 = args.n2
+    n = n2 // 2
+    dev = torch.device("cuda", local)
+
+    # synthetic input (per-rank seed), master copy resident in HBM
+    d_host = inputs.random_matrix(n, 1000 + rank)
+    master = torch.from_numpy(np.ascontiguousarray(d_host.T)).to(dev)      # (n2, n2) = column-major D
+    work = torch.empty_like(master)
+    deig = torch.zeros(n2, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        work[:n].copy_(master[:n])  # restore the left half (columns 0..n-1 of D)
+        rc = solver.zquatev_device(work, deig, stream)
+        if rc != 0:
+            raise RuntimeError(f"zquatev_device rc={rc}: {_lib.last_error()}")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # timed region: K steps, events on the launching stream; kernel classes profiled
+    lib.zq_profile_reset()
+    lib.zq_profile_enable((1 << 1) | (1 << 0) | (1 << 3) | (1 << 4) | (1 << 5) | (1 << 6) | (1 << 7))
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    lib.zq_profile_enable(0)
+    ms_total = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    prof = {k: _lib.profile_read(k) for k in ("hemv", "trail", "formq_gemm", "apply_z", "stedc", "tridiag", "formq")}
+
+    # accuracy of the last device solve (GPU residual; FP64 torch matmul as checker)
+    acc = {}
+    if not args.no_check:
+        out = work
+        eig = deig[:n]
+        h = torch.from_numpy(inputs.full_from_blocks(d_host[:n, :n], d_host[n:, :n])).to(dev)
+        v = out.T  # column-major view
+        acc = {"residual": metrics.torch_residual(h, v, eig), "orthonormality": metrics.torch_orthonormality(v)}
+        del h
+
+    # end to end through the host C ABI (H2D + solve + D2H inside)
+    e2e_ms = []
+    for _ in range(args.e2e_steps):
+        dh = d_host.copy(order="F")
+        eh = np.zeros(n2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = solver.zquatev(n2, dh, n2, eh)
+        t1 = time.perf_counter()
+        assert rc == 0, _lib.last_error()
+        e2e_ms.append((t1 - t0) * 1e3)
+    e2e = float(np.mean(e2e_ms))
+
+    # roofline: dominant kernel class by event time
+    F = {  # executed FP64 flops per solve for each class (4M complex multiply-add = 8 flops, 3M = 6)
+        "trail": (16.0 / 3.0) * n ** 3 * 2,              # 32 n^3/3 DFMA-equivalent flops (4M, lower triangles)
+        "hemv": (16.0 / 3.0) * n ** 3 * 2,               # 4 complex matvecs per column on the lower triangles
+        "formq_gemm": 8.0 * n ** 3 * 2,                  # (8/3) n^3 CMAC in 3M = 8 n^3 DFMA
+        "apply_z": 8.0 * n ** 3,                         # (4n x n) x (n x n) real
+    }
+    per_step = {k: prof[k][0] / args.steps for k in prof}
+    dom = max(("trail", "hemv", "formq_gemm", "apply_z"), key=lambda k: per_step[k])
+    dom_ms = per_step[dom]
+    launches = prof[dom][1] / max(args.steps, 1)
+    achieved = F[dom] / (dom_ms * 1e-3) / 1e12 if dom_ms > 0 else None
+    peak = fp64_peak_tflops()
+
+    if rank == 0:
+        cpu_ms, cpu_raw = cpu_sample(args.cpu_sample_n2, n2, os.cpu_count() or 1)
+        clocks = clk.summary()
+        line = {
+            "metric": METRIC,
+            "value": ms_step,
+            "unit": "ms",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": False,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"single quaternion-Hermitian solve n2={n2} (n={n}), random A=(X+X^H)/2, "
+                                   "B=(Y-Y^T)/2, complex128, all eigenvectors, plain FP64 path",
+                       "n2": n2, "nb": int(lib.zq_get_block_size()), "parallelism": f"replicas{world}",
+                       "l2": "inputs (512 MiB left half) larger than L2; restored D2D each step"},
+            "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": n2 * n * 16,
+                    "d2h_bytes_per_step": n2 * n2 * 16 + n * 8},
+            "gpu_launches": None,
+            "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
+                         "peak_source": "measured in this run: DFMA calibration kernel (no FP64 peak in MEASURED_PEAKS.json)",
+                         "launches_per_step": launches, "ms_per_step": dom_ms},
+            "stage_ms": {k: round(v, 3) for k, v in per_step.items()},
+            "accuracy": acc,
+            "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": os.cpu_count() or 1, "kind": "port",
+                             "sample": f"one n2={args.cpu_sample_n2} solve through oracle/port.py (numpy + scipy "
+                                       f"OpenBLAS/LAPACK) = {cpu_raw:.2f} s, scaled x{(n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
+            "clocks": clocks,
+        }
+        # kernel launches per step: counted by the profiler brackets are classes only; report the
+        # library's own launch count for one solve of this size
+        line["gpu_launches"] = launches_per_solve(n) * args.steps
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def launches_per_solve(n: int, nb: int = 32, nbq: int = 64) -> int:
+    """Kernel launches of one vectors solve (counted from the launch sequence)."""
+    cnt = 0
+    for p in range(0, n, nb):
+        nbp = min(nb, n - p)
+        for k in range(nbp):
+            j = p + k
+            L = n - 1 - j
+            cnt += 1
+            if L < 1:
+                continue
+            cnt += 1 + (1 if (L >= 2 and k > 0) else 0) + (1 if L >= 2 else 0) + 1
+        if p + nbp < n:
+            cnt += 2
+    cnt += 1  # phase
+    # D&C: per depth leaf + 6 kernels; plus scale/unscale
+    depth = 0
+    m = n
+    while m > 1:
+        m = (m + 1) // 2
+        depth += 1
+    cnt += 4 + 7 * (depth + 1)
+    # Q formation: init + per block (pack, build_t, 8 GEMMs (+ up to 8 split reduces))
+    nref = max(n - 2, 0)
+    cnt += 1 + ((nref + nbq - 1) // nbq) * (2 + 8 + 4)
+    cnt += 2  # apply_z, symfill
+    return cnt
+
+
+if __name__ == "__main__":
+    main()

@@ -60,6 +60,16 @@ int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const lon
 int zq_set_block_size(int nb);
 int zq_get_block_size(void);
 
+/* Kernel-class timing with CUDA events on the launching streams (for the
+ * benchmark's roofline figures; off by default, adds two event records per
+ * bracketed launch). Classes: 0 quaternion hemv, 1 trailing update, 2 panel
+ * column kernels, 3 Q-formation GEMMs, 4 back-transform GEMM, 5 tridiagonal
+ * eigensolver, 6 whole tridiagonalisation, 7 whole Q formation, 8 batched
+ * kernel. No reference counterpart. */
+int zq_profile_enable(int mask);
+int zq_profile_read(int cls, double* total_ms, long long* launches);
+int zq_profile_reset(void);
+
 /* Frees the cached device workspace of the current device. */
 int zq_release_workspace(void);
 

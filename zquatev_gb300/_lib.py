@@ -21,6 +21,9 @@ SIGNATURES = {
     "zquatev_values_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
     "zq_stedc_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),
     "zquatev_batched_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "zq_profile_enable": (_c_int, [_c_int]),
+    "zq_profile_read": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
+    "zq_profile_reset": (_c_int, []),
     "zq_set_block_size": (_c_int, [_c_int]),
     "zq_get_block_size": (_c_int, []),
     "zq_release_workspace": (_c_int, []),
@@ -63,3 +66,14 @@ def check(rc: int, what: str) -> int:
     if rc < 0:
         raise ZquatevError(f"{what} returned {rc}: {last_error()}")
     return rc
+
+
+PROFILE_CLASSES = {"hemv": 0, "trail": 1, "panel": 2, "formq_gemm": 3, "apply_z": 4, "stedc": 5,
+                   "tridiag": 6, "formq": 7, "batched": 8}
+
+
+def profile_read(name: str) -> tuple[float, int]:
+    ms = ctypes.c_double()
+    cnt = ctypes.c_longlong()
+    check(load().zq_profile_read(PROFILE_CLASSES[name], ctypes.byref(ms), ctypes.byref(cnt)), "zq_profile_read")
+    return ms.value, cnt.value

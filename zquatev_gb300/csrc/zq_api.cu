@@ -41,6 +41,56 @@ const char* last_error_message() { return g_last_error.c_str(); }
 static void set_msg(const char* m) { g_last_error = m; }
 
 // ----------------------------------------------------------------------------
+// per-kernel-class event timing
+// ----------------------------------------------------------------------------
+struct Prof {
+  std::mutex mu;
+  int mask = 0;
+  struct Pair { cudaEvent_t a, b; int cls; };
+  std::vector<Pair> pairs;
+  std::vector<cudaEvent_t> pool;
+  int open_idx[PC_COUNT];
+  double total_ms[PC_COUNT];
+  long long launches[PC_COUNT];
+  Prof() { for (int i = 0; i < PC_COUNT; ++i) { open_idx[i] = -1; total_ms[i] = 0; launches[i] = 0; } }
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e; cudaEventCreate(&e); return e;
+  }
+  void collect() {
+    for (auto& p : pairs) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+        total_ms[p.cls] += ms;
+        launches[p.cls] += 1;
+      }
+      pool.push_back(p.a); pool.push_back(p.b);
+    }
+    pairs.clear();
+  }
+};
+static Prof g_prof;
+
+void prof_begin(int cls, cudaStream_t st) {
+  if (!(g_prof.mask & (1 << cls))) return;
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  Prof::Pair p{g_prof.get(), nullptr, cls};
+  cudaEventRecord(p.a, st);
+  g_prof.open_idx[cls] = (int)g_prof.pairs.size();
+  g_prof.pairs.push_back(p);
+}
+void prof_end(int cls, cudaStream_t st) {
+  if (!(g_prof.mask & (1 << cls))) return;
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  const int i = g_prof.open_idx[cls];
+  if (i < 0) return;
+  g_prof.pairs[i].b = g_prof.get();
+  cudaEventRecord(g_prof.pairs[i].b, st);
+  g_prof.open_idx[cls] = -1;
+  if (g_prof.pairs.size() > 16384) g_prof.collect();
+}
+
+// ----------------------------------------------------------------------------
 // per-device context: streams, events, growable workspace, cached D&C plan
 // ----------------------------------------------------------------------------
 struct Context {
@@ -57,7 +107,7 @@ struct Context {
 static std::mutex g_ctx_mu;
 static Context* g_ctx[64];
 static int g_nb = 32;   // panel width (autotuned table may override per n)
-static int g_nbq = 32;  // Q-formation block
+static int g_nbq = 64;  // Q-formation block
 
 static int nb_for(int n) {
   if (const char* s = getenv("ZQ_NB")) { const int v = atoi(s); if (v >= 1 && v <= 64) return v; }
@@ -175,7 +225,9 @@ static int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* dei
 
   tm.mark("start", c->st);
   TridiagView<double> v = tridiag_bind<double>(tri_ws, dD, n, ldd, 64, d, e, tau);
+  prof_begin(PC_TRIDIAG, c->st);
   if (int rc = tridiagonalize<double>(v, nb, c->st)) return rc;
+  prof_end(PC_TRIDIAG, c->st);
   if (int rc = phase_reduce(e, n, offd, phi, c->st)) return rc;
   tm.mark("tridiag", c->st);
 
@@ -184,10 +236,14 @@ static int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* dei
     ZQ_CUDA(cudaEventRecord(c->ev_fork, c->st));
     ZQ_CUDA(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
     double2* X = dD + (int64_t)n * ldd;  // right half as workspace (as the reference does)
+    prof_begin(PC_FORMQ, c->st2);
     if (int rc = form_q(dD, ldd, n, phi, X, ldd, nbq, fq_ws, c->st2)) return rc;
+    prof_end(PC_FORMQ, c->st2);
     ZQ_CUDA(cudaEventRecord(c->ev_join, c->st2));
     double* Z = nullptr;
+    prof_begin(PC_STEDC, c->st);
     if (int rc = c->dc.run(d, offd, lam, Z, c->st)) return rc;
+    prof_end(PC_STEDC, c->st);
     tm.mark("stedc", c->st);
     ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_join, 0));
     tm.mark("formq-wait", c->st);
@@ -338,6 +394,28 @@ int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const lon
   if (count == 0) return ZQ_OK;
   return batched_solve(count, n2s, ld2s, offs, eoffs, reinterpret_cast<double2*>(dD), deig,
                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zq_profile_enable(int mask) {
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  g_prof.mask = mask;
+  return ZQ_OK;
+}
+
+int zq_profile_read(int cls, double* total_ms, long long* launches) {
+  if (cls < 0 || cls >= PC_COUNT || !total_ms || !launches) { set_msg("bad profile class"); return ZQ_ERR_ARG; }
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  g_prof.collect();
+  *total_ms = g_prof.total_ms[cls];
+  *launches = g_prof.launches[cls];
+  return ZQ_OK;
+}
+
+int zq_profile_reset(void) {
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  g_prof.collect();
+  for (int i = 0; i < PC_COUNT; ++i) { g_prof.total_ms[i] = 0; g_prof.launches[i] = 0; }
+  return ZQ_OK;
 }
 
 int zq_set_block_size(int nb) {

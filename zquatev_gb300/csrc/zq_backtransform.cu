@@ -86,32 +86,51 @@ __global__ void k_pack_w(const double2* M, int64_t ldm, int n, int p, int kb, in
 }
 
 // T (kb x kb quaternion, upper triangular) from G1 = <w_i, w_l>, G2 = [w_i, w_l]:
-//   T[k][k] = 1,  T[i][k] = - sum_{l<k} T[i][l] q(G1[l][k], G2[l][k])
-__global__ void k_build_t(const double2* G1, const double2* G2, int kb, double2* Ta, double2* Tb) {
-  const int i = threadIdx.x;
-  for (int t = i; t < kb * kb; t += blockDim.x) { Ta[t] = make_double2(0.0, 0.0); Tb[t] = make_double2(0.0, 0.0); }
+//   T[k][k] = 1,  T[i][k] = - sum_{i<=l<k} T[i][l] q(G1[l][k], G2[l][k])
+// One CTA of 1024 threads: thread (i, g) sums the l = i+g, i+g+16, ... terms of
+// column k; the 16 partials of each row are reduced in shared memory.
+constexpr int BT_G = 16;
+__global__ void __launch_bounds__(1024) k_build_t(const double2* G1, const double2* G2, int kb, double2* Ta, double2* Tb) {
+  const int tid = threadIdx.x;
+  const int i = tid & 63, g = tid >> 6;
+  __shared__ double2 red[BT_G][64][2];
+  for (int t = tid; t < kb * kb; t += blockDim.x) { Ta[t] = make_double2(0.0, 0.0); Tb[t] = make_double2(0.0, 0.0); }
   __syncthreads();
   for (int k = 0; k < kb; ++k) {
+    double2 sa = make_double2(0.0, 0.0), sb = sa;
     if (i < k) {
-      double2 sa = make_double2(0.0, 0.0), sb = sa;
-      for (int l = i; l < k; ++l) {
+      for (int l = i + g; l < k; l += BT_G) {
         const double2 ta = Ta[i + l * kb], tb = Tb[i + l * kb];
         const double2 g1 = G1[l + k * kb], g2 = G2[l + k * kb];
         // q(ta, tb) q(g1, g2) = q(ta g1 - conj(tb) g2, tb g1 + conj(ta) g2)
         cfma(sa, ta, g1); cfmac(sa, cneg(tb), g2);
         cfma(sb, tb, g1); cfmac(sb, ta, g2);
       }
-      Ta[i + k * kb] = cneg(sa);
-      Tb[i + k * kb] = cneg(sb);
     }
-    if (i == k) { Ta[k + k * kb] = make_double2(1.0, 0.0); Tb[k + k * kb] = make_double2(0.0, 0.0); }
+    red[g][i][0] = sa;
+    red[g][i][1] = sb;
+    __syncthreads();
+    if (g == 0) {
+      if (i < k) {
+        double2 ta = make_double2(0.0, 0.0), tb = ta;
+        for (int q = 0; q < BT_G; ++q) { ta = cadd(ta, red[q][i][0]); tb = cadd(tb, red[q][i][1]); }
+        Ta[i + k * kb] = cneg(ta);
+        Tb[i + k * kb] = cneg(tb);
+      } else if (i == k) {
+        Ta[k + k * kb] = make_double2(1.0, 0.0);
+        Tb[k + k * kb] = make_double2(0.0, 0.0);
+      }
+    }
     __syncthreads();
   }
 }
 
+// split-K partial buffer of the Q formation (complex elements)
+static int64_t fq_pcap(int n, int nbq) { return (int64_t)16 * nbq * (n > 64 ? n : 64); }
+
 size_t form_q_workspace_bytes(int n, int nbq) {
-  // Wa, Wb (n x nbq), G1, G2, Ta, Tb (nbq^2), C1e, C1o, C2e, C2o (nbq x n)
-  return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n) + 256;
+  // Wa, Wb (n x nbq), G1, G2, Ta, Tb (nbq^2), C1e, C1o, C2e, C2o (nbq x n), split-K partials
+  return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n + (size_t)fq_pcap(n, nbq)) + 256;
 }
 
 int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, int64_t ldx, int nbq, void* ws,
@@ -131,7 +150,9 @@ int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, 
   double2* C1e = p; p += (size_t)nbq * n;
   double2* C1o = p; p += (size_t)nbq * n;
   double2* C2e = p; p += (size_t)nbq * n;
-  double2* C2o = p;
+  double2* C2o = p; p += (size_t)nbq * n;
+  double2* Pk = p;
+  const int64_t pcap = fq_pcap(n, nbq);
   double2* Xa = X;
   double2* Xb = X + n;
   const int nblocks = ceil_div(nref, nbq);
@@ -142,8 +163,10 @@ int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, 
     k_pack_w<<<ceil_div(L * kb, 256) > 2048 ? 2048 : ceil_div(L * kb, 256), 256, 0, st>>>(M, ldm, n, pb, kb, L, Wa, Wb);
     ZQ_LAUNCH_CHECK();
     ZgemmArgs g{};
+    g.P = Pk; g.pcap = pcap;
     // G1 = Wa^H Wa + Wb^H Wb ; G2 = Wa^T Wb - Wb^T Wa   (kb x kb, inner L)
     g = ZgemmArgs{};
+    g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = kb; g.k1 = L; g.k2 = L;
     g.A1 = Wa; g.lda1 = L; g.B1 = Wa; g.ldb1 = L;
     g.A2 = Wb; g.lda2 = L; g.B2 = Wb; g.ldb2 = L;
@@ -152,12 +175,13 @@ int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, 
     if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
     g.A1 = Wa; g.B1 = Wb; g.A2 = Wb; g.B2 = Wa; g.s2 = -1.0; g.C = G2;
     if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
-    k_build_t<<<1, 64, 0, st>>>(G1, G2, kb, Ta, Tb);
+    k_build_t<<<1, 1024, 0, st>>>(G1, G2, kb, Ta, Tb);
     ZQ_LAUNCH_CHECK();
     // C1e = Wa^H Xa_sub + Wb^H Xb_sub ; C1o = Wa^T Xb_sub - Wb^T Xa_sub   (kb x L)
     double2* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
     double2* Xbs = Xb + (pb + 1) + (int64_t)(pb + 1) * ldx;
     g = ZgemmArgs{};
+    g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = L; g.k1 = L; g.k2 = L;
     g.A1 = Wa; g.lda1 = L; g.B1 = Xas; g.ldb1 = ldx;
     g.A2 = Wb; g.lda2 = L; g.B2 = Xbs; g.ldb2 = ldx;
@@ -168,6 +192,7 @@ int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, 
     if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
     // C2e = Ta C1e - conj(Tb) C1o ; C2o = Tb C1e + conj(Ta) C1o   (kb x L)
     g = ZgemmArgs{};
+    g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = L; g.k1 = kb; g.k2 = kb;
     g.A1 = Ta; g.lda1 = kb; g.B1 = C1e; g.ldb1 = kb;
     g.A2 = Tb; g.lda2 = kb; g.B2 = C1o; g.ldb2 = kb;
@@ -178,6 +203,7 @@ int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, 
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
     // Xa_sub -= Wa C2e - conj(Wb) C2o ; Xb_sub -= Wb C2e + conj(Wa) C2o   (L x L)
     g = ZgemmArgs{};
+    g.P = Pk; g.pcap = pcap;
     g.m = L; g.n = L; g.k1 = kb; g.k2 = kb;
     g.A1 = Wa; g.lda1 = L; g.B1 = C2e; g.ldb1 = kb;
     g.A2 = Wb; g.lda2 = L; g.B2 = C2o; g.ldb2 = kb;
@@ -199,7 +225,10 @@ int apply_z(const double2* X, int64_t ldx, const double* Z, int64_t ldz, int n, 
   d.C = reinterpret_cast<double*>(out); d.ldc = 2 * ldo;
   d.m = 4 * n; d.n = n; d.k = n;
   d.alpha = 1.0; d.beta = 0.0;
-  return dgemm_grouped(&d, 1, dev_desc, st);
+  prof_begin(PC_APPLYZ, st);
+  const int rc = dgemm_grouped(&d, 1, dev_desc, st);
+  prof_end(PC_APPLYZ, st);
+  return rc;
 }
 
 __global__ void k_symfill(double2* D, int64_t ld, int n) {

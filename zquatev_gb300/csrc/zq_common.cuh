@@ -123,6 +123,16 @@ enum Status : int {
 void set_last_error(cudaError_t e, const char* what, const char* file, int line);
 const char* last_error_message();
 
+// Optional per-kernel-class timing with CUDA events recorded on the launching
+// stream (off unless enabled through zq_profile_enable). Each begin/end pair
+// brackets one launch; totals are read back after a synchronisation.
+enum ProfClass : int {
+  PC_HEMV = 0, PC_TRAIL = 1, PC_PANEL = 2, PC_FORMQ_GEMM = 3, PC_APPLYZ = 4,
+  PC_STEDC = 5, PC_TRIDIAG = 6, PC_FORMQ = 7, PC_BATCHED = 8, PC_COUNT = 9
+};
+void prof_begin(int cls, cudaStream_t st);
+void prof_end(int cls, cudaStream_t st);
+
 inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -43,12 +43,12 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
   const int tid = threadIdx.x;
   const int tr = tid & 15, tc = tid >> 4;
   const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
-  const int bz = blockIdx.z;
-  const double2* A1 = g.A1 + bz * g.sA1;
-  const double2* B1 = g.B1 + bz * g.sB1;
-  const double2* A2 = g.A2 ? g.A2 + bz * g.sA2 : nullptr;
-  const double2* B2 = g.B2 ? g.B2 + bz * g.sB2 : nullptr;
-  double2* C = g.C + bz * g.sC;
+  const int split = blockIdx.z;
+  const double2* A1 = g.A1;
+  const double2* B1 = g.B1;
+  const double2* A2 = g.A2;
+  const double2* B2 = g.B2;
+  double2* C = g.C;
   double t1[4][4], t2[4][4], t3[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
@@ -59,7 +59,10 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
   for (int seg = 0; seg < nseg; ++seg) {
     const int K = seg == 0 ? g.k1 : g.k2;
     const double sgn = seg == 0 ? 1.0 : g.s2;
-    for (int k0 = 0; k0 < K; k0 += GK) {
+    // this split's share of the segment, in whole GK steps
+    const int steps = (K + GK - 1) / GK;
+    const int sb = (int)(((int64_t)steps * split) / gridDim.z), se = (int)(((int64_t)steps * (split + 1)) / gridDim.z);
+    for (int k0 = sb * GK; k0 < se * GK; k0 += GK) {
       __syncthreads();
       for (int e = tid; e < GK * GT; e += GNT) {
         // A tile: 64 rows x GK; B tile: GK x 64 cols
@@ -100,6 +103,22 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
       }
     }
   }
+  if (gridDim.z > 1) {
+    // raw partial sums; k_zsplit_reduce applies alpha/beta
+    double2* P = g.P + (int64_t)split * g.m * g.n;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int i = i0 + tr + 16 * a;
+      if (i >= g.m) continue;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const int j = j0 + tc + 16 * b;
+        if (j >= g.n) continue;
+        P[i + (int64_t)j * g.m] = make_double2(t1[a][b] - t2[a][b], t3[a][b] - t1[a][b] - t2[a][b]);
+      }
+    }
+    return;
+  }
   const double2 al = g.alpha, be = g.beta;
   const bool use_beta = (be.x != 0.0 || be.y != 0.0);
 #pragma unroll
@@ -124,12 +143,54 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
   }
 }
 
+__global__ void k_zsplit_reduce(ZgemmArgs g, int splits) {
+  const int64_t total = (int64_t)g.m * g.n;
+  const bool use_beta = (g.beta.x != 0.0 || g.beta.y != 0.0);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < splits; ++s) {
+      const double2 p = g.P[t + (int64_t)s * total];
+      re += p.x; im += p.y;
+    }
+    const int i = (int)(t % g.m), j = (int)(t / g.m);
+    double2 out = make_double2(g.alpha.x * re - g.alpha.y * im, g.alpha.x * im + g.alpha.y * re);
+    const int64_t o = i + (int64_t)j * g.ldc;
+    if (use_beta) {
+      const double2 c = g.C[o];
+      out.x += g.beta.x * c.x - g.beta.y * c.y;
+      out.y += g.beta.x * c.y + g.beta.y * c.x;
+    }
+    g.C[o] = out;
+  }
+}
+
+// Split the K range over enough CTAs to fill the GPU when the output is small
+// (e.g. the 64 x L products of the Q formation); partials go to g.P.
+static int choose_splits(const ZgemmArgs& g) {
+  if (!g.P || g.pcap <= 0) return 1;
+  const int tiles = ceil_div(g.m, GT) * ceil_div(g.n, GT);
+  const int ksteps = ceil_div(g.k1, GK) + (g.A2 ? ceil_div(g.k2, GK) : 0);
+  int s = 1;
+  while (tiles * s < 2 * 152 && ksteps / (2 * s) >= 16 && (int64_t)(2 * s) * g.m * g.n <= g.pcap) s *= 2;
+  return s;
+}
+
 template <int OPA1, int OPB1, int OPA2, int OPB2>
 int zgemm_launch(const ZgemmArgs& g, int batch, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0) return ZQ_OK;
-  dim3 grid(ceil_div(g.m, GT), ceil_div(g.n, GT), batch);
+  (void)batch;
+  const int splits = choose_splits(g);
+  dim3 grid(ceil_div(g.m, GT), ceil_div(g.n, GT), splits);
+  prof_begin(PC_FORMQ_GEMM, st);
   k_zgemm<OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
+  prof_end(PC_FORMQ_GEMM, st);
   ZQ_LAUNCH_CHECK();
+  if (splits > 1) {
+    const int64_t total = (int64_t)g.m * g.n;
+    const int blocks = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
+    k_zsplit_reduce<<<blocks, 256, 0, st>>>(g, splits);
+    ZQ_LAUNCH_CHECK();
+  }
   return ZQ_OK;
 }
 

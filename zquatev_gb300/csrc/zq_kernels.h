@@ -45,13 +45,14 @@ enum { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };
 
 struct ZgemmArgs {
   int m, n, k1, k2;
-  const double2* A1; int64_t lda1; int64_t sA1;
-  const double2* B1; int64_t ldb1; int64_t sB1;
-  const double2* A2; int64_t lda2; int64_t sA2;
-  const double2* B2; int64_t ldb2; int64_t sB2;
+  const double2* A1; int64_t lda1;
+  const double2* B1; int64_t ldb1;
+  const double2* A2; int64_t lda2;   // null: single segment
+  const double2* B2; int64_t ldb2;
   double s2;
   double2 alpha, beta;
-  double2* C; int64_t ldc; int64_t sC;
+  double2* C; int64_t ldc;
+  double2* P; int64_t pcap;          // optional split-K partial buffer (complex elements)
 };
 int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, int batch, cudaStream_t st);
 

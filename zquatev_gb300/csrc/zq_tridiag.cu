@@ -45,8 +45,9 @@
 
 namespace zq {
 
-constexpr int RB = 64;        // rows per CTA for the row-parallel kernels
-constexpr int TB = 64;        // tile edge for hemv / trailing update
+constexpr int RB = 32;        // rows per CTA for the row-parallel kernels
+constexpr int NG = 8;         // reflector groups per CTA in the row kernels (NT / RB)
+constexpr int TB = 64;        // tile edge of the trailing update
 constexpr int NT = 256;       // threads per CTA
 
 // ----------------------------------------------------------------------------
@@ -61,21 +62,19 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   Z* B = v.M + n;
   const int r0 = j + blockIdx.x * RB;
   const int tid = threadIdx.x;
-  const int row = tid & (RB - 1);   // 0..63
-  const int grp = tid >> 6;         // 0..3
+  const int row = tid & (RB - 1);
+  const int grp = tid >> 5;
   const int r = r0 + row;
   __shared__ Z s_sc[4 * 64];        // per i: ya_i[j], yb_i[j], wa_i[j], wb_i[j]
-  __shared__ Z s_red[4][RB][2];
+  __shared__ Z s_red[NG][RB][2];
   __shared__ double s_red_d[2][NT / 32];
   __shared__ double s_c;
 
   // c_{k-1} = sum of partials (deterministic order)
-  if (k > 0) {
-    if (tid == 0) {
-      double c = 0;
-      for (int i = 0; i < ncp; ++i) c += v.cpart[i];
-      s_c = c;
-    }
+  if (k > 0 && tid == 0) {
+    double c = 0;
+    for (int i = 0; i < ncp; ++i) c += v.cpart[i];
+    s_c = c;
   }
   __syncthreads();
   const R half_c = (k > 0) ? (R)(0.5 * s_c) : (R)0;
@@ -83,32 +82,29 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   // finish y_{k-1} = g - (c/2) w_{k-1} on this CTA's rows (rows >= j)
   if (k > 0 && grp == 0 && r < n) {
     const Z wa = A[r + (int64_t)(j - 1) * ld], wb = B[r + (int64_t)(j - 1) * ld];
-    const Z ga = v.ga[r], gb = v.gb[r];
-    v.Ya[r + (int64_t)(k - 1) * v.ldy] = csub(ga, cscale(wa, half_c));
-    v.Yb[r + (int64_t)(k - 1) * v.ldy] = csub(gb, cscale(wb, half_c));
+    v.Ya[r + (int64_t)(k - 1) * v.ldy] = csub(v.ga[r], cscale(wa, half_c));
+    v.Yb[r + (int64_t)(k - 1) * v.ldy] = csub(v.gb[r], cscale(wb, half_c));
   }
   if (!do_update) return;
 
   // scalars at row j for every previous reflector of the panel
-  if (k > 0) {
-    for (int i = tid; i < k; i += NT) {
-      Z ya, yb;
-      const Z wa = A[j + (int64_t)(p + i) * ld], wb = B[j + (int64_t)(p + i) * ld];
-      if (i == k - 1) {
-        ya = csub(v.ga[j], cscale(wa, half_c));
-        yb = csub(v.gb[j], cscale(wb, half_c));
-      } else {
-        ya = v.Ya[j + (int64_t)i * v.ldy];
-        yb = v.Yb[j + (int64_t)i * v.ldy];
-      }
-      s_sc[4 * i + 0] = ya; s_sc[4 * i + 1] = yb; s_sc[4 * i + 2] = wa; s_sc[4 * i + 3] = wb;
+  for (int i = tid; i < k; i += NT) {
+    Z ya, yb;
+    const Z wa = A[j + (int64_t)(p + i) * ld], wb = B[j + (int64_t)(p + i) * ld];
+    if (i == k - 1) {
+      ya = csub(v.ga[j], cscale(wa, half_c));
+      yb = csub(v.gb[j], cscale(wb, half_c));
+    } else {
+      ya = v.Ya[j + (int64_t)i * v.ldy];
+      yb = v.Yb[j + (int64_t)i * v.ldy];
     }
+    s_sc[4 * i + 0] = ya; s_sc[4 * i + 1] = yb; s_sc[4 * i + 2] = wa; s_sc[4 * i + 3] = wb;
   }
   __syncthreads();
 
   Z da = czero<Z>(), db = czero<Z>();
-  if (k > 0 && r < n) {
-    for (int i = grp; i < k; i += 4) {
+  if (r < n) {
+    for (int i = grp; i < k; i += NG) {
       const Z sya = s_sc[4 * i + 0], syb = s_sc[4 * i + 1], swa = s_sc[4 * i + 2], swb = s_sc[4 * i + 3];
       const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
       Z ya, yb;
@@ -133,7 +129,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   Z xa = czero<Z>(), xb = czero<Z>();
   if (grp == 0 && r < n) {
     Z ta = s_red[0][row][0], tb = s_red[0][row][1];
-    for (int g2 = 1; g2 < 4; ++g2) { ta = cadd(ta, s_red[g2][row][0]); tb = cadd(tb, s_red[g2][row][1]); }
+    for (int g2 = 1; g2 < NG; ++g2) { ta = cadd(ta, s_red[g2][row][0]); tb = cadd(tb, s_red[g2][row][1]); }
     xa = csub(A[r + (int64_t)j * ld], ta);
     xb = csub(B[r + (int64_t)j * ld], tb);
     A[r + (int64_t)j * ld] = xa;
@@ -217,35 +213,35 @@ __global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, 
   const double f = s_sc[0];
   const int r0 = j + 1 + blockIdx.x * RB;
   const int row = tid & (RB - 1);
-  const int grp = tid >> 6;
+  const int grp = tid >> 5;
   const int r = r0 + row;
-  Z wa = czero<Z>(), wb = czero<Z>();
-  if (grp == 0 && r < n) {
-    if (f > 0.0) {
-      if (r == j + 1) {
-        wa = mk((R)s_sc[1], (R)s_sc[2]);
-        wb = mk((R)s_sc[3], (R)s_sc[4]);
-      } else {
-        wa = cscale(A[r + (int64_t)j * ld], (R)f);
-        wb = cscale(B[r + (int64_t)j * ld], (R)f);
+  __shared__ Z s_wa[RB], s_wb[RB];
+  if (grp == 0) {
+    Z wa = czero<Z>(), wb = czero<Z>();
+    if (r < n) {
+      if (f > 0.0) {
+        if (r == j + 1) {
+          wa = mk((R)s_sc[1], (R)s_sc[2]);
+          wb = mk((R)s_sc[3], (R)s_sc[4]);
+        } else {
+          wa = cscale(A[r + (int64_t)j * ld], (R)f);
+          wb = cscale(B[r + (int64_t)j * ld], (R)f);
+        }
       }
+      A[r + (int64_t)j * ld] = wa;
+      B[r + (int64_t)j * ld] = wb;
     }
-    A[r + (int64_t)j * ld] = wa;
-    B[r + (int64_t)j * ld] = wb;
+    s_wa[row] = wa; s_wb[row] = wb;
   }
-
   // dot partials vs previous reflectors / aux vectors of the panel
   if (k == 0 || L < 2) return;
-  __shared__ Z s_wa[RB], s_wb[RB];
-  if (grp == 0) { s_wa[row] = wa; s_wb[row] = wb; }
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31;
+  const int gr = r0 + lane;
+  const Z xa = s_wa[lane], xb = s_wb[lane];
   for (int i = warp; i < k; i += NT / 32) {
     Z d1 = czero<Z>(), d2 = czero<Z>(), d3 = czero<Z>(), d4 = czero<Z>();
-    for (int rr = lane; rr < RB; rr += 32) {
-      const int gr = r0 + rr;
-      if (gr >= n) break;
-      const Z xa = s_wa[rr], xb = s_wb[rr];
+    if (gr < n) {
       const Z ya = v.Ya[gr + (int64_t)i * v.ldy], yb = v.Yb[gr + (int64_t)i * v.ldy];
       const Z qa = A[gr + (int64_t)(p + i) * ld], qb = B[gr + (int64_t)(p + i) * ld];
       // <y,w> = ya^H xa + yb^H xb ; [y,w] = ya^T xb - yb^T xa
@@ -281,173 +277,167 @@ __global__ void k_dotsum(TridiagView<R> v, int k, int ndp) {
 
 // ----------------------------------------------------------------------------
 // hemv: quaternion Hermitian mat-vec of the panel-start trailing matrix.
-//   Region rows/cols [r0, n); lower-triangle 64x64 tiles, one CTA per tile.
-//   Outputs per 64-row block R and source block S the partial sums of
-//   v0 = A x, v1 = A z, v2 = B x, v3 = B z  with x = wa, z = conj(wb).
+//   Region rows/cols [r0, n); lower-triangle 32x32 tiles, one CTA per tile.
+//   The A and B tiles are staged in shared memory (padded, conflict-free for
+//   both row and column sweeps) and four warps each own one product:
+//     warp 0: rows,  A x and A z          warp 2: columns, A^H x and A^H z
+//     warp 1: rows,  B x and B z          warp 3: columns, -B^T x and -B^T z
+//   (x = wa, z = conj(wb)), so every lower-triangle element is read once from
+//   HBM and used for its row and its (conjugate-)transposed column without any
+//   cross-thread reduction: all FP64 work is DFMA. Per T-row block R and source
+//   block S the CTA stores the partial sums of v0 = A x, v1 = A z, v2 = B x,
+//   v3 = B z.
 // ----------------------------------------------------------------------------
+constexpr int HT = 32;        // hemv tile edge
+constexpr int HLD = HT + 1;   // padded shared leading dimension
 template <typename R>
-__global__ void __launch_bounds__(NT) k_hemv(TridiagView<R> v, int j) {
+__global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
   const Z* A = v.M;
   const Z* B = v.M + n;
   const int r0 = j + 1;
-  // tile index -> (I, J) with I >= J
   const int t = blockIdx.x;
   int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
   while ((I + 1) * (I + 2) / 2 <= t) ++I;
   while (I * (I + 1) / 2 > t) --I;
   const int J = t - I * (I + 1) / 2;
-  const int tid = threadIdx.x;
-  const int tr = tid & 15, tc = tid >> 4;
-  const int rbase = r0 + I * TB + 4 * tr;
-  const int cbase = r0 + J * TB + 4 * tc;
-
-  Z xr[4], zr[4], xc[4], zc[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int gr = rbase + q, gc = cbase + q;
-    if (gr < n) { xr[q] = A[gr + (int64_t)j * ld]; zr[q] = cconj(B[gr + (int64_t)j * ld]); }
-    else { xr[q] = czero<Z>(); zr[q] = czero<Z>(); }
-    if (gc < n) { xc[q] = A[gc + (int64_t)j * ld]; zc[q] = cconj(B[gc + (int64_t)j * ld]); }
-    else { xc[q] = czero<Z>(); zc[q] = czero<Z>(); }
-  }
-  Z dr[4][4], dc[4][4];  // [row/col][vector]
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int u = 0; u < 4; ++u) { dr[q][u] = czero<Z>(); dc[q][u] = czero<Z>(); }
-
   const bool diag = (I == J);
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    const int gc = cbase + c;
-    if (gc >= n) continue;
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int gr = rbase + q;
-      if (gr >= n) continue;
-      if (diag && gr < gc) continue;
-      Z a = A[gr + (int64_t)gc * ld];
-      Z b = B[gr + (int64_t)gc * ld];
-      if (gr == gc) { a.y = 0; b = czero<Z>(); }
-      // direct (row gr)
-      cfma(dr[q][0], a, xc[c]); cfma(dr[q][1], a, zc[c]);
-      cfma(dr[q][2], b, xc[c]); cfma(dr[q][3], b, zc[c]);
-      if (gr > gc) {
-        // transposed (row gc): conj(a) x_r, conj(a) z_r, -b x_r, -b z_r
-        cfmac(dc[c][0], a, xr[q]); cfmac(dc[c][1], a, zr[q]);
-        const Z nb_ = cneg(b);
-        cfma(dc[c][2], nb_, xr[q]); cfma(dc[c][3], nb_, zr[q]);
-      }
+  const int tid = threadIdx.x;
+  const int rbase = r0 + I * HT, cbase = r0 + J * HT;
+  __shared__ Z sA[HT * HLD], sB[HT * HLD];
+  __shared__ Z sx[2][HT], sz[2][HT];   // [0]: rows of block I, [1]: rows of block J
+  __shared__ Z sout[HT][4];
+  for (int e = tid; e < HT * HT; e += 128) {
+    const int r = e & (HT - 1), c = e >> 5;
+    const int gr = rbase + r, gc = cbase + c;
+    Z a = czero<Z>(), b = czero<Z>();
+    if (gr < n && gc < n && (!diag || r >= c)) {
+      a = A[gr + (int64_t)gc * ld];
+      b = B[gr + (int64_t)gc * ld];
+      if (diag && r == c) { a.y = 0; b = czero<Z>(); }
     }
+    sA[r + c * HLD] = a;
+    sB[r + c * HLD] = b;
   }
-  // column partials: reduce over tr (16 lanes of a half-warp)
-#pragma unroll
-  for (int c = 0; c < 4; ++c)
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      R x = dc[c][u].x, y = dc[c][u].y;
-#pragma unroll
-      for (int o = 8; o > 0; o >>= 1) {
-        x += __shfl_xor_sync(0xffffffffu, x, o);
-        y += __shfl_xor_sync(0xffffffffu, y, o);
-      }
-      dc[c][u].x = x; dc[c][u].y = y;
-    }
-  // row partials: first pair-reduce tc within a warp (lanes l and l^16)
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      dr[q][u].x += __shfl_xor_sync(0xffffffffu, dr[q][u].x, 16);
-      dr[q][u].y += __shfl_xor_sync(0xffffffffu, dr[q][u].y, 16);
-    }
-  __shared__ Z s_row[8][TB][4];   // [warp][row][vector]
-  __shared__ Z s_col[TB][4];
-  const int warp = tid >> 5, lane = tid & 31;
-  if (lane < 16) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-#pragma unroll
-      for (int u = 0; u < 4; ++u) s_row[warp][4 * tr + q][u] = dr[q][u];
-  }
-  if (tr == 0) {
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-      for (int u = 0; u < 4; ++u) s_col[4 * tc + c][u] = dc[c][u];
+  if (tid < 2 * HT) {
+    const int s = tid >> 5, q = tid & (HT - 1);
+    const int g = (s == 0 ? rbase : cbase) + q;
+    Z x = czero<Z>(), z = czero<Z>();
+    if (g < n) { x = A[g + (int64_t)j * ld]; z = cconj(B[g + (int64_t)j * ld]); }
+    sx[s][q] = x;
+    sz[s][q] = z;
   }
   __syncthreads();
-  const int orow = tid >> 2, ou = tid & 3;
-  Z sr = czero<Z>();
-#pragma unroll
-  for (int w = 0; w < 8; ++w) sr = cadd(sr, s_row[w][orow][ou]);
-  const int nbm = v.hblk;  // partial grid stride (blocks)
-  if (diag) {
-    sr = cadd(sr, s_col[orow][ou]);
-    v.hpart[(((int64_t)I * nbm + I) * TB + orow) * 4 + ou] = sr;
+  const int role = tid >> 5, q = tid & (HT - 1);
+  // two accumulators per product (even / odd k) for independent FMA chains
+  Z p0 = czero<Z>(), p1 = czero<Z>(), p2 = czero<Z>(), p3 = czero<Z>();
+  if (role < 2) {
+    const Z* S = role == 0 ? sA : sB;
+#pragma unroll 8
+    for (int c = 0; c < HT; c += 2) {
+      const Z m0 = S[q + c * HLD], m1 = S[q + (c + 1) * HLD];
+      cfma(p0, m0, sx[1][c]); cfma(p1, m0, sz[1][c]);
+      cfma(p2, m1, sx[1][c + 1]); cfma(p3, m1, sz[1][c + 1]);
+    }
+  } else if (role == 2) {
+    for (int r = diag ? q + 1 : 0; r < HT; ++r) {
+      const Z m = sA[r + q * HLD];
+      if (r & 1) { cfmac(p2, m, sx[0][r]); cfmac(p3, m, sz[0][r]); }
+      else { cfmac(p0, m, sx[0][r]); cfmac(p1, m, sz[0][r]); }
+    }
   } else {
-    v.hpart[(((int64_t)I * nbm + J) * TB + orow) * 4 + ou] = sr;
-    v.hpart[(((int64_t)J * nbm + I) * TB + orow) * 4 + ou] = s_col[orow][ou];
+    for (int r = diag ? q + 1 : 0; r < HT; ++r) {
+      const Z m = sB[r + q * HLD];
+      if (r & 1) { cfma(p2, m, sx[0][r]); cfma(p3, m, sz[0][r]); }
+      else { cfma(p0, m, sx[0][r]); cfma(p1, m, sz[0][r]); }
+    }
+    p0 = cneg(p0); p1 = cneg(p1); p2 = cneg(p2); p3 = cneg(p3);
+  }
+  const Z u0 = cadd(p0, p2), u1 = cadd(p1, p3);   // this warp's two products
+  const int nbm = v.hblk;
+  if (role >= 2) {
+    if (diag) { sout[q][2 * (role - 2)] = u0; sout[q][2 * (role - 2) + 1] = u1; }
+    else {
+      Z* o = v.hpart + (((int64_t)J * nbm + I) * HT + q) * 4 + 2 * (role - 2);
+      o[0] = u0; o[1] = u1;
+    }
+  }
+  if (diag) __syncthreads();
+  if (role < 2) {
+    Z a0 = u0, a1 = u1;
+    if (diag) { a0 = cadd(a0, sout[q][2 * role]); a1 = cadd(a1, sout[q][2 * role + 1]); }
+    Z* o = v.hpart + (((int64_t)I * nbm + J) * HT + q) * 4 + 2 * role;
+    o[0] = a0; o[1] = a1;
   }
 }
 
 // ----------------------------------------------------------------------------
 // hreduce: g = H_panelstart w - corrections, for rows [j+1, n); c partials.
+//   T is the hemv tile edge used for this column; nblk its number of blocks.
 // ----------------------------------------------------------------------------
 template <typename R>
-__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int nblk, int zero_mode) {
+__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode) {
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
   const Z* A = v.M;
   const Z* B = v.M + n;
   const int r0 = j + 1;
-  const int Rb = blockIdx.x;
   const int tid = threadIdx.x;
-  __shared__ Z s_v[TB][4];
+  const int row = tid & (RB - 1), grp = tid >> 5;
+  const int lrow = blockIdx.x * RB + row;   // row index inside the region
+  const int r = r0 + lrow;
+  __shared__ Z s_v[RB][4];
   __shared__ Z s_dots[4 * 64];
-  __shared__ double s_red[NT / 32];
-  const int orow = tid >> 2, ou = tid & 3;
-  if (!zero_mode) {
+  __shared__ Z s_red[NG][RB][2];
+  __shared__ double s_redd[NT / 32];
+  if (!zero_mode && tid < 4 * RB) {
+    const int orow = tid >> 2, ou = tid & 3;
+    const int lr = blockIdx.x * RB + orow;
     Z s = czero<Z>();
-    const int nbm = v.hblk;
-    for (int S = 0; S < nblk; ++S) s = cadd(s, v.hpart[(((int64_t)Rb * nbm + S) * TB + orow) * 4 + ou]);
+    if (r0 + lr < n) {
+      const int Rb = lr / T, off = lr % T;
+      const int nbm = v.hblk;
+      for (int S = 0; S < nblk; ++S) s = cadd(s, v.hpart[(((int64_t)Rb * nbm + S) * T + off) * 4 + ou]);
+    }
     s_v[orow][ou] = s;
   }
   for (int t = tid; t < 4 * k; t += NT) s_dots[t] = v.dots[t];
   __syncthreads();
-  double cp = 0.0;
-  if (tid < TB) {
-    const int r = r0 + Rb * TB + tid;
-    if (r < n) {
-      Z ga = czero<Z>(), gb = czero<Z>();
-      if (!zero_mode) {
-        // ha = A x - conj(B z), hb = B x + conj(A z)
-        ga = csub(s_v[tid][0], cconj(s_v[tid][3]));
-        gb = cadd(s_v[tid][2], cconj(s_v[tid][1]));
-        for (int i = 0; i < k; ++i) {
-          const Z s1 = s_dots[4 * i + 0], s2 = s_dots[4 * i + 1], s3 = s_dots[4 * i + 2], s4 = s_dots[4 * i + 3];
-          const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
-          const Z ya = v.Ya[r + (int64_t)i * v.ldy], yb = v.Yb[r + (int64_t)i * v.ldy];
-          // ga -= wa s1 - conj(wb) s2 + ya s3 - conj(yb) s4
-          // gb -= wb s1 + conj(wa) s2 + yb s3 + conj(ya) s4
-          Z ta = czero<Z>(), tb = czero<Z>();
-          cfma(ta, wa, s1); cfmac(ta, cneg(wb), s2); cfma(ta, ya, s3); cfmac(ta, cneg(yb), s4);
-          cfma(tb, wb, s1); cfmac(tb, wa, s2); cfma(tb, yb, s3); cfmac(tb, ya, s4);
-          ga = csub(ga, ta); gb = csub(gb, tb);
-        }
-        const Z wa = A[r + (int64_t)j * ld], wb = B[r + (int64_t)j * ld];
-        cp = (double)(wa.x * ga.x + wa.y * ga.y + wb.x * gb.x + wb.y * gb.y);
-      }
-      v.ga[r] = ga;
-      v.gb[r] = gb;
+  // deferred-update corrections, reflectors split over the groups
+  Z ta = czero<Z>(), tb = czero<Z>();
+  if (!zero_mode && r < n) {
+    for (int i = grp; i < k; i += NG) {
+      const Z s1 = s_dots[4 * i + 0], s2 = s_dots[4 * i + 1], s3 = s_dots[4 * i + 2], s4 = s_dots[4 * i + 3];
+      const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
+      const Z ya = v.Ya[r + (int64_t)i * v.ldy], yb = v.Yb[r + (int64_t)i * v.ldy];
+      // ga -= wa s1 - conj(wb) s2 + ya s3 - conj(yb) s4
+      // gb -= wb s1 + conj(wa) s2 + yb s3 + conj(ya) s4
+      cfma(ta, wa, s1); cfmac(ta, cneg(wb), s2); cfma(ta, ya, s3); cfmac(ta, cneg(yb), s4);
+      cfma(tb, wb, s1); cfmac(tb, wa, s2); cfma(tb, yb, s3); cfmac(tb, ya, s4);
     }
   }
-  const double bs = block_sum(cp, s_red);
-  if (tid == 0) v.cpart[Rb] = bs;
+  s_red[grp][row][0] = ta;
+  s_red[grp][row][1] = tb;
+  __syncthreads();
+  double cp = 0.0;
+  if (grp == 0 && r < n) {
+    Z ga = czero<Z>(), gb = czero<Z>();
+    if (!zero_mode) {
+      // ha = A x - conj(B z), hb = B x + conj(A z)
+      ga = csub(s_v[row][0], cconj(s_v[row][3]));
+      gb = cadd(s_v[row][2], cconj(s_v[row][1]));
+      for (int g2 = 0; g2 < NG; ++g2) { ga = csub(ga, s_red[g2][row][0]); gb = csub(gb, s_red[g2][row][1]); }
+      const Z wa = A[r + (int64_t)j * ld], wb = B[r + (int64_t)j * ld];
+      cp = (double)(wa.x * ga.x + wa.y * ga.y + wb.x * gb.x + wb.y * gb.y);
+    }
+    v.ga[r] = ga;
+    v.gb[r] = gb;
+  }
+  const double bs = block_sum(cp, s_redd);
+  if (tid == 0) v.cpart[blockIdx.x] = bs;
 }
 
 // ----------------------------------------------------------------------------
@@ -558,33 +548,45 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
       const int j = p + k;
       const int L = n - 1 - j;
       const int ncta1 = ceil_div(n - j, RB);
+      prof_begin(PC_PANEL, st);
       k_colupd<R><<<ncta1, NT, 0, st>>>(v, p, j, k, ncp, 1);
       ZQ_LAUNCH_CHECK();
-      if (L < 1) { ncp = 0; continue; }
+      if (L < 1) { prof_end(PC_PANEL, st); ncp = 0; continue; }
       const int ncta2 = ceil_div(L, RB);
       k_reflect<R><<<ncta2, NT, 0, st>>>(v, p, j, k, ncta1);
       ZQ_LAUNCH_CHECK();
-      const int nblk = ceil_div(L, TB);
-      if (L >= 2) {
-        if (k > 0) {
-          k_dotsum<R><<<1, NT, 0, st>>>(v, k, ncta2);
-          ZQ_LAUNCH_CHECK();
-        }
-        k_hemv<R><<<nblk * (nblk + 1) / 2, NT, 0, st>>>(v, j);
+      const int T = HT;
+      const int nblk = ceil_div(L, T);
+      if (L >= 2 && k > 0) {
+        k_dotsum<R><<<1, NT, 0, st>>>(v, k, ncta2);
         ZQ_LAUNCH_CHECK();
       }
-      k_hreduce<R><<<nblk, NT, 0, st>>>(v, p, j, k, nblk, L < 2 ? 1 : 0);
+      prof_end(PC_PANEL, st);
+      if (L >= 2) {
+        prof_begin(PC_HEMV, st);
+        k_hemv<R><<<nblk * (nblk + 1) / 2, 128, 0, st>>>(v, j);
+        ZQ_LAUNCH_CHECK();
+        prof_end(PC_HEMV, st);
+      }
+      prof_begin(PC_PANEL, st);
+      const int nhr = ceil_div(L, RB);
+      k_hreduce<R><<<nhr, NT, 0, st>>>(v, p, j, k, T, nblk, L < 2 ? 1 : 0);
       ZQ_LAUNCH_CHECK();
-      ncp = nblk;
+      prof_end(PC_PANEL, st);
+      ncp = nhr;
     }
     const int t0 = p + nbp;
     if (t0 < n) {
       // finish y of the panel's last reflector (rows >= t0), then update
+      prof_begin(PC_PANEL, st);
       k_colupd<R><<<ceil_div(n - t0, RB), NT, 0, st>>>(v, p, t0, nbp, ncp, 0);
       ZQ_LAUNCH_CHECK();
+      prof_end(PC_PANEL, st);
       const int nblk = ceil_div(n - t0, TB);
+      prof_begin(PC_TRAIL, st);
       k_trail<R><<<nblk * (nblk + 1) / 2, NT, 0, st>>>(v, p, nbp, t0);
       ZQ_LAUNCH_CHECK();
+      prof_end(PC_TRAIL, st);
       ncp = 0;
     }
   }
@@ -594,11 +596,11 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
 template <typename R>
 size_t tridiag_workspace_bytes(int n, int nbmax) {
   using Z = cplx<R>;
-  const size_t hblk = (size_t)ceil_div(n > 0 ? n : 1, TB);
+  const size_t hblk = (size_t)ceil_div(n > 0 ? n : 1, 32);
   size_t b = 0;
   b += sizeof(Z) * (2 * (size_t)n * nbmax);          // Ya, Yb
   b += sizeof(Z) * (2 * (size_t)n);                   // ga, gb
-  b += sizeof(Z) * (hblk * hblk * TB * 4);            // hpart
+  b += sizeof(Z) * ((hblk + 2) * (hblk + 2) * 32 * 4);  // hpart: 32-tiles, or 64-tiles at the same block stride
   b += sizeof(Z) * (hblk * nbmax * 4);                // dpart
   b += sizeof(Z) * (4 * (size_t)nbmax);               // dots
   b += sizeof(double) * (3 * hblk + 8);               // npart, cpart, scal
@@ -609,7 +611,7 @@ template <typename R>
 TridiagView<R> tridiag_bind(void* ws, cplx<R>* M, int n, int64_t ld, int nbmax, double* d, double* e, double* tau) {
   using Z = cplx<R>;
   TridiagView<R> v{};
-  const int hblk = ceil_div(n > 0 ? n : 1, TB);
+  const int hblk = ceil_div(n > 0 ? n : 1, 32);
   char* p = reinterpret_cast<char*>(ws);
   auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~(size_t)255; return q; };
   v.M = M; v.n = n; v.ld = ld; v.nbmax = nbmax; v.ldy = n > 0 ? n : 1; v.hblk = hblk;
@@ -617,7 +619,7 @@ TridiagView<R> tridiag_bind(void* ws, cplx<R>* M, int n, int64_t ld, int nbmax, 
   v.Yb = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)n * nbmax));
   v.ga = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)n));
   v.gb = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)n));
-  v.hpart = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)hblk * hblk * TB * 4));
+  v.hpart = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)(hblk + 2) * (hblk + 2) * 32 * 4));
   v.dpart = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)hblk * nbmax * 4));
   v.dots = reinterpret_cast<Z*>(take(sizeof(Z) * 4 * (size_t)nbmax));
   v.npart = reinterpret_cast<double*>(take(sizeof(double) * 2 * hblk));
