@@ -49,9 +49,12 @@ int zq_stedc_device(int n, const double* d, const double* e, double* lam, double
 /* Batched solve of `count` independent matrices held in device memory:
  * matrix b has order n2s[b] (even), starts at dD + 2*offs[b] doubles
  * (complex offset offs[b]) with leading dimension ld2s[b], and eigenvalues at
- * deig + eoffs[b]. All arrays n2s/ld2s/offs/eoffs are HOST arrays. The whole
- * batch runs as one persistent kernel launch ordered after `stream`.
- * No reference counterpart (the reference solves one matrix per call). */
+ * deig + eoffs[b]. All arrays n2s/ld2s/offs/eoffs are HOST arrays. Matrices
+ * with n2 <= 512 run in one persistent kernel launch (one CTA per matrix,
+ * largest first); larger ones through the per-matrix path. Ordered after
+ * `stream`; returns after the batch has finished, with the largest per-matrix
+ * info (0 = all converged). The reference solves one matrix per call; this has
+ * no counterpart there. */
 int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const long long* offs,
                            const long long* eoffs, double* dD, double* deig, void* stream);
 

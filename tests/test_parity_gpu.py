@@ -198,3 +198,68 @@ def test_larger_random(gpu):
     d = inputs.random_matrix(n, 4242)
     out, eig = run(d)
     check_solution(d, out, eig, n)
+
+
+def _batch(sizes, seed0):
+    """Pack matrices of quaternion orders `sizes` into one device buffer."""
+    import torch
+
+    offs, eoffs, n2s, ld2s, mats = [], [], [], [], []
+    off = eoff = 0
+    for i, n in enumerate(sizes):
+        d = inputs.random_matrix(n, seed0 + i)
+        mats.append(d)
+        n2s.append(2 * n)
+        ld2s.append(2 * n)
+        offs.append(off)
+        eoffs.append(eoff)
+        off += 4 * n * n
+        eoff += 2 * n
+    buf = np.zeros(max(off, 1), dtype=np.complex128)
+    for d, o in zip(mats, offs):
+        buf[o:o + d.size] = d.ravel(order="F")
+    dbuf = torch.from_numpy(buf).cuda()
+    deig = torch.zeros(max(eoff, 1), dtype=torch.float64, device="cuda")
+    return mats, offs, eoffs, n2s, ld2s, dbuf, deig
+
+
+def _run_batch(lib, sizes, seed0):
+    import ctypes
+
+    import torch
+
+    mats, offs, eoffs, n2s, ld2s, dbuf, deig = _batch(sizes, seed0)
+    c = len(sizes)
+    rc = lib.zquatev_batched_device(c, (ctypes.c_int * c)(*n2s), (ctypes.c_int * c)(*ld2s),
+                                    (ctypes.c_longlong * c)(*offs), (ctypes.c_longlong * c)(*eoffs),
+                                    dbuf.data_ptr(), deig.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, (rc, _lib.last_error())
+    torch.cuda.synchronize()
+    out = dbuf.cpu().numpy()
+    ev = deig.cpu().numpy()
+    res = []
+    for d, o, eo, n2 in zip(mats, offs, eoffs, n2s):
+        res.append((d, out[o:o + d.size].reshape(d.shape, order="F"), ev[eo:eo + n2]))
+    return res
+
+
+def test_batched_uneven(gpu):
+    rng = np.random.default_rng(9)
+    sizes = [int(x) for x in np.floor(np.exp(rng.uniform(np.log(1), np.log(260), 60)))]
+    sizes += [1, 2, 3, 255, 256, 257]
+    for d, out, eig in _run_batch(gpu, sizes, 500):
+        n = d.shape[1] // 2
+        check_solution(d, out, eig, n)
+
+
+def test_batched_equals_single(gpu):
+    """Batched result == per-matrix drop-in result within the tolerance."""
+    sizes = [40, 17, 96]
+    for d, out, eig in _run_batch(gpu, sizes, 900):
+        n = d.shape[1] // 2
+        sout, seig = run(d)
+        h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
+        hn = metrics.h_norm2(seig[:n])
+        assert metrics.eig_error(eig[:n], seig[:n], hn) <= TOL
+        assert metrics.subspace_distance(out, eig[:n], sout, seig[:n], 1e-6 * hn) < 1e-8
+        assert metrics.residual(h, out, eig[:n]) <= TOL

@@ -21,6 +21,7 @@
 #include "zq_kernels.h"
 #include "../../include/zquatev_gb300.h"
 
+#include <algorithm>
 #include <complex>
 #include <cstdlib>
 #include <cstring>
@@ -306,17 +307,81 @@ static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors) 
   return rc;
 }
 
-// Batched: every matrix solved on the device through the per-matrix path.
+// ----------------------------------------------------------------------------
+// batched: small matrices (n <= batched_max_n()) in one persistent kernel,
+// larger ones through the per-matrix path on the same stream
+// ----------------------------------------------------------------------------
+long long batched_ws_stride();
+int batched_max_n();
+int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
+                   int ctas, int* dev_info, cudaStream_t st);
+size_t batched_task_bytes();
+void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot);
+
+struct BatchBuffers {
+  void* dev = nullptr;
+  size_t bytes = 0;
+  std::vector<char> host_tasks;
+};
+static BatchBuffers g_batch[64];
+static int g_batch_ctas_per_sm = 2;
+
 static int batched_solve(int count, const int* n2s, const int* ld2s, const long long* offs, const long long* eoffs,
                          double2* dD, double* deig, cudaStream_t st) {
   Context* c = nullptr;
   if (int rc = get_context(&c)) return rc;
   std::lock_guard<std::mutex> lk(c->mu);
+  const int nmax = batched_max_n();
+  // small tasks, largest first (longest-processing-time order)
+  std::vector<int> small, large;
   for (int b = 0; b < count; ++b) {
     if (n2s[b] == 0) continue;
+    ((n2s[b] / 2 <= nmax) ? small : large).push_back(b);
+  }
+  std::stable_sort(small.begin(), small.end(), [&](int x, int y) { return n2s[x] > n2s[y]; });
+  int info_max = 0;
+  if (!small.empty()) {
+    int sms = 0;
+    ZQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    const char* env = getenv("ZQ_BATCH_CTAS_PER_SM");
+    const int per_sm = env ? atoi(env) : g_batch_ctas_per_sm;
+    int ctas = sms * (per_sm > 0 ? per_sm : 2);
+    if (ctas > (int)small.size()) ctas = (int)small.size();
+    const size_t tb = batched_task_bytes();
+    const size_t task_bytes = align256(tb * small.size());
+    const size_t info_bytes = align256(sizeof(int) * small.size() + sizeof(int));
+    const size_t ws_bytes = sizeof(double) * (size_t)batched_ws_stride() * ctas;
+    const size_t need = task_bytes + info_bytes + ws_bytes;
+    BatchBuffers& bb = g_batch[c->device];
+    if (bb.bytes < need) {
+      if (bb.dev) { cudaStreamSynchronize(c->st); cudaFree(bb.dev); bb.dev = nullptr; bb.bytes = 0; }
+      ZQ_CUDA(cudaMalloc(&bb.dev, need));
+      bb.bytes = need;
+    }
+    char* base = reinterpret_cast<char*>(bb.dev);
+    void* dtasks = base;
+    int* dinfo = reinterpret_cast<int*>(base + task_bytes);
+    int* dcounter = dinfo + small.size();
+    double* dws = reinterpret_cast<double*>(base + task_bytes + info_bytes);
+    bb.host_tasks.resize(tb * small.size());
+    for (size_t q = 0; q < small.size(); ++q) {
+      const int b = small[q];
+      batched_fill_task(bb.host_tasks.data() + q * tb, offs[b], eoffs[b], n2s[b] / 2, ld2s[b], (int)q);
+    }
+    ZQ_CUDA(cudaEventRecord(c->ev_fork, st));
+    ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
+    ZQ_CUDA(cudaMemcpyAsync(dtasks, bb.host_tasks.data(), tb * small.size(), cudaMemcpyHostToDevice, c->st));
+    if (int rc = batched_launch(dtasks, (int)small.size(), dcounter, dD, deig, dws, ctas, dinfo, c->st)) return rc;
+    std::vector<int> hinfo(small.size());
+    ZQ_CUDA(cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(int) * small.size(), cudaMemcpyDeviceToHost, c->st));
+    ZQ_CUDA(cudaStreamSynchronize(c->st));
+    for (int v : hinfo) info_max = v > info_max ? v : info_max;
+  }
+  for (int b : large) {
     if (int rc = solve_device(c, dD + offs[b], ld2s[b], n2s[b] / 2, deig + eoffs[b], true, st)) return rc;
   }
-  return ZQ_OK;
+  ZQ_CUDA(cudaStreamSynchronize(st));
+  return info_max;
 }
 
 }  // namespace zq

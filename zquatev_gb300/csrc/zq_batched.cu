@@ -1,0 +1,375 @@
+// Batched solve of many small quaternion-Hermitian matrices in ONE persistent
+// kernel launch (one CTA per matrix, work handed out largest-first through a
+// device counter).
+//
+// Reference: the same four steps as ts::zquatev (zquatev.cc:42-100) run once
+// per matrix; the reference has no batched entry point, and below n = nb + 2
+// it runs only its unblocked path (unblocked.cc:44-131), which is the regime
+// of this kernel. Per matrix, inside one CTA (FP64 throughout):
+//   1. unblocked quaternion tridiagonalisation of [A; B] in place: per column
+//      one quaternion reflector (same construction as zq_tridiag.cu), the
+//      quaternion Hermitian mat-vec g = H w on the trailing lower triangles
+//      (thread per row), y = g - (w^H g / 2) w and the structured rank-2
+//      update of the trailing lower triangles of A and B; w is kept in the
+//      reduced column;
+//   2. phase reduction of the quaternion subdiagonal (unit quaternions);
+//   3. implicit QL with Wilkinson shifts on the real tridiagonal, rotations of
+//      each sweep recorded by one thread and applied to the rows of Z by all
+//      threads (classic tql2 scheme);
+//   4. X = Phi Z (ascending eigenvalue order) in the right half of D, the
+//      reflectors applied backwards (warp per column, coalesced over rows),
+//      then the (U -V*; V U*) layout written out.
+#include "zq_common.cuh"
+#include "zq_kernels.h"
+
+namespace zq {
+
+constexpr int BT = 256;        // threads per CTA
+constexpr int BNMAX = 256;     // largest quaternion order handled in one CTA
+
+struct BatchTask {
+  long long off;    // complex offset of D
+  long long eoff;   // offset of eig
+  int n, ld;
+  int out_slot;     // index into the info array
+  int pad;
+};
+
+struct BatchArgs {
+  const BatchTask* tasks;
+  int count;
+  int* counter;     // work counter (zeroed before the launch)
+  double2* D;
+  double* eig;
+  double* ws;       // per-CTA workspace, slot stride ws_stride doubles
+  long long ws_stride;
+  int* info;        // per task: 0 ok, >0 QL non-convergence
+};
+
+__device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double* ws) {
+  const int n = tk.n;
+  const int64_t ld = tk.ld;
+  double2* A = a.D + tk.off;
+  double2* B = A + n;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  __shared__ double2 swa[BNMAX], swb[BNMAX], sya[BNMAX], syb[BNMAX];
+  __shared__ double sred[BT / 32];
+  __shared__ double sscal[8];
+  __shared__ double sc_[BNMAX], ss_[BNMAX];   // QL rotations of one sweep
+  __shared__ int sflag[2];
+  double* d = ws;                 // n
+  double* e4 = d + BNMAX;         // 4n quaternion subdiagonal
+  double* offd = e4 + 4 * BNMAX;  // n
+  double* phi = offd + BNMAX;     // 4n
+  double* rank_d = phi + 4 * BNMAX;  // n (eigenvalues, QL output)
+  int* perm = reinterpret_cast<int*>(rank_d + BNMAX);  // n
+  double* Z = rank_d + 2 * BNMAX;  // n x n, column-major, ld n
+
+  // ---------------------------------------------------------------- step 1
+  for (int j = 0; j < n; ++j) {
+    const int L = n - 1 - j;
+    if (tid == 0) d[j] = A[j + (int64_t)j * ld].x;
+    if (L < 1) break;
+    // norm of x = (A[j+1:, j], B[j+1:, j]) (max-scaled)
+    double mx = 0.0;
+    for (int i = tid; i < L; i += BT) {
+      const double2 xa = A[j + 1 + i + (int64_t)j * ld], xb = B[j + 1 + i + (int64_t)j * ld];
+      mx = fmax(mx, fmax(fmax(fabs(xa.x), fabs(xa.y)), fmax(fabs(xb.x), fabs(xb.y))));
+    }
+    mx = block_max(mx, sred);
+    double ssq = 0.0;
+    if (mx > 0.0) {
+      const double inv = 1.0 / mx;
+      for (int i = tid; i < L; i += BT) {
+        const double2 xa = A[j + 1 + i + (int64_t)j * ld], xb = B[j + 1 + i + (int64_t)j * ld];
+        const double a0 = xa.x * inv, a1 = xa.y * inv, b0 = xb.x * inv, b1 = xb.y * inv;
+        ssq += a0 * a0 + a1 * a1 + b0 * b0 + b1 * b1;
+      }
+    }
+    ssq = block_sum(ssq, sred);
+    if (tid == 0) {
+      const double nu = mx * sqrt(ssq);
+      const double2 qa = A[j + 1 + (int64_t)j * ld], qb = B[j + 1 + (int64_t)j * ld];
+      const double q1 = sqrt(qa.x * qa.x + qa.y * qa.y + qb.x * qb.x + qb.y * qb.y);
+      double f = 0.0, m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+      double ee0 = qa.x, ee1 = qa.y, ee2 = qb.x, ee3 = qb.y;
+      if (L >= 2) {
+        if (nu > 0.0) {
+          if (q1 > 0.0) {
+            const double s = nu / q1;
+            f = 1.0 / (sqrt(nu) * sqrt(nu + q1));
+            m0 = qa.x * (1 + s); m1 = qa.y * (1 + s); m2 = qb.x * (1 + s); m3 = qb.y * (1 + s);
+            ee0 = -s * qa.x; ee1 = -s * qa.y; ee2 = -s * qb.x; ee3 = -s * qb.y;
+          } else {
+            f = 1.0 / nu; m0 = nu;
+            ee0 = -nu; ee1 = 0; ee2 = 0; ee3 = 0;
+          }
+        } else {
+          ee0 = ee1 = ee2 = ee3 = 0.0;
+        }
+      }
+      e4[4 * j] = ee0; e4[4 * j + 1] = ee1; e4[4 * j + 2] = ee2; e4[4 * j + 3] = ee3;
+      sscal[0] = f; sscal[1] = m0 * f; sscal[2] = m1 * f; sscal[3] = m2 * f; sscal[4] = m3 * f;
+    }
+    __syncthreads();
+    const double f = sscal[0];
+    // w in place of x (and in shared memory)
+    for (int i = tid; i < L; i += BT) {
+      double2 wa = make_double2(0, 0), wb = wa;
+      if (f > 0.0) {
+        if (i == 0) { wa = make_double2(sscal[1], sscal[2]); wb = make_double2(sscal[3], sscal[4]); }
+        else { wa = cscale(A[j + 1 + i + (int64_t)j * ld], f); wb = cscale(B[j + 1 + i + (int64_t)j * ld], f); }
+      }
+      A[j + 1 + i + (int64_t)j * ld] = wa;
+      B[j + 1 + i + (int64_t)j * ld] = wb;
+      swa[i] = wa; swb[i] = wb;
+    }
+    __syncthreads();
+    if (f == 0.0) continue;
+    // g = H_trail w  (rows j+1.., thread per row; lower triangles only)
+    const int r0 = j + 1;
+    double cp = 0.0;
+    for (int i = tid; i < L; i += BT) {
+      double2 ax = make_double2(0, 0), az = ax, bx = ax, bz = ax;
+      const int gi = r0 + i;
+      for (int c = 0; c < L; ++c) {
+        const int gc = r0 + c;
+        const double2 x = swa[c], z = cconj(swb[c]);
+        if (c < i) {
+          const double2 am = A[gi + (int64_t)gc * ld], bm = B[gi + (int64_t)gc * ld];
+          cfma(ax, am, x); cfma(az, am, z); cfma(bx, bm, x); cfma(bz, bm, z);
+        } else if (c == i) {
+          const double am = A[gi + (int64_t)gi * ld].x;
+          ax.x += am * x.x; ax.y += am * x.y; az.x += am * z.x; az.y += am * z.y;
+        } else {
+          const double2 am = A[gc + (int64_t)gi * ld], bm = B[gc + (int64_t)gi * ld];
+          cfmac(ax, am, x); cfmac(az, am, z);           // conj(A[c,i])
+          cfma(bx, cneg(bm), x); cfma(bz, cneg(bm), z); // B[i,c] = -B[c,i]
+        }
+      }
+      // ga = A x - conj(B z), gb = B x + conj(A z)
+      const double2 ga = csub(ax, cconj(bz)), gb = cadd(bx, cconj(az));
+      sya[i] = ga; syb[i] = gb;
+      cp += swa[i].x * ga.x + swa[i].y * ga.y + swb[i].x * gb.x + swb[i].y * gb.y;
+    }
+    const double c = block_sum(cp, sred);
+    for (int i = tid; i < L; i += BT) {
+      sya[i] = csub(sya[i], cscale(swa[i], 0.5 * c));
+      syb[i] = csub(syb[i], cscale(swb[i], 0.5 * c));
+    }
+    __syncthreads();
+    // rank-2 structured update of the trailing lower triangles
+    for (int cc = 0; cc < L; ++cc) {
+      const double2 wac = swa[cc], wbc = swb[cc], yac = sya[cc], ybc = syb[cc];
+      const int gc = r0 + cc;
+      for (int i = cc + tid; i < L; i += BT) {
+        const double2 wai = swa[i], wbi = swb[i], yai = sya[i], ybi = syb[i];
+        double2 ta = make_double2(0, 0), tb = ta;
+        cfmacb(ta, wai, yac); cfmac(ta, wbi, ybc); cfmacb(ta, yai, wac); cfmac(ta, ybi, wbc);
+        const int64_t o = (r0 + i) + (int64_t)gc * ld;
+        A[o] = csub(A[o], ta);
+        if (i > cc) {
+          cfmacb(tb, wbi, yac); cfmac(tb, cneg(wai), ybc); cfmacb(tb, ybi, wac); cfmac(tb, cneg(yai), wbc);
+          B[o] = csub(B[o], tb);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- step 2
+  if (tid == 0) {
+    double a0 = 1.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;
+    phi[0] = a0; phi[1] = a1; phi[2] = b0; phi[3] = b1;
+    for (int k = 0; k + 1 < n; ++k) {
+      const double ea0 = e4[4 * k], ea1 = e4[4 * k + 1], eb0 = e4[4 * k + 2], eb1 = e4[4 * k + 3];
+      const double nrm = sqrt(ea0 * ea0 + ea1 * ea1 + eb0 * eb0 + eb1 * eb1);
+      offd[k] = nrm;
+      if (nrm > 0.0) {
+        const double na0 = (ea0 * a0 - ea1 * a1) - (eb0 * b0 + eb1 * b1);
+        const double na1 = (ea0 * a1 + ea1 * a0) - (eb0 * b1 - eb1 * b0);
+        const double nb0 = (eb0 * a0 - eb1 * a1) + (ea0 * b0 + ea1 * b1);
+        const double nb1 = (eb0 * a1 + eb1 * a0) + (ea0 * b1 - ea1 * b0);
+        const double s = 1.0 / sqrt(na0 * na0 + na1 * na1 + nb0 * nb0 + nb1 * nb1);
+        a0 = na0 * s; a1 = na1 * s; b0 = nb0 * s; b1 = nb1 * s;
+      } else {
+        a0 = 1.0; a1 = 0.0; b0 = 0.0; b1 = 0.0;
+      }
+      phi[4 * (k + 1)] = a0; phi[4 * (k + 1) + 1] = a1; phi[4 * (k + 1) + 2] = b0; phi[4 * (k + 1) + 3] = b1;
+    }
+    offd[n - 1] = 0.0;
+    sflag[0] = 0;
+  }
+  // Z = I
+  for (int t = tid; t < n * n; t += BT) Z[t] = ((t % n) == (t / n)) ? 1.0 : 0.0;
+  __syncthreads();
+
+  // ---------------------------------------------------------------- step 3
+  // implicit QL with Wilkinson shift; d <- eigenvalues, Z <- eigenvectors
+  const double eps = 1.1102230246251565e-16;
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0;; ++iter) {
+      __shared__ int s_m, s_cnt, s_done;
+      if (tid == 0) {
+        int m = l;
+        for (; m < n - 1; ++m) {
+          const double dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(offd[m]) <= eps * dd || fabs(offd[m]) < 1e-300) break;
+        }
+        s_done = (m == l) || (iter >= 60);
+        if (iter >= 60 && m != l) sflag[0] += 1;
+        s_cnt = 0;
+        if (!s_done) {
+          double g = (d[l + 1] - d[l]) / (2.0 * offd[l]);
+          double r = hypot(g, 1.0);
+          g = d[m] - d[l] + offd[l] / (g + copysign(r, g));
+          double s = 1.0, c = 1.0, p = 0.0;
+          int i = m - 1;
+          bool early = false;
+          for (; i >= l; --i) {
+            const double ff = s * offd[i], bb = c * offd[i];
+            r = hypot(ff, g);
+            offd[i + 1] = r;
+            if (r == 0.0) { d[i + 1] -= p; offd[m] = 0.0; early = true; break; }
+            s = ff / r; c = g / r;
+            g = d[i + 1] - p;
+            r = (d[i] - g) * s + 2.0 * c * bb;
+            p = s * r;
+            d[i + 1] = g + p;
+            g = c * r - bb;
+            sc_[s_cnt] = c; ss_[s_cnt] = s; ++s_cnt;
+          }
+          if (!early) { d[l] -= p; offd[l] = g; offd[m] = 0.0; }
+          s_m = m;
+        }
+      }
+      __syncthreads();
+      if (s_done) break;
+      // apply the sweep's rotations (columns m-1 .. lo of Z) to every row
+      const int m = s_m, cnt = s_cnt;
+      for (int r = tid; r < n; r += BT) {
+        double* zr = Z + r;
+        for (int q = 0; q < cnt; ++q) {
+          const int i = m - 1 - q;
+          const double c = sc_[q], s = ss_[q];
+          const double zi = zr[(int64_t)i * n], zi1 = zr[(int64_t)(i + 1) * n];
+          zr[(int64_t)(i + 1) * n] = s * zi + c * zi1;
+          zr[(int64_t)i * n] = c * zi - s * zi1;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // ascending order: rank of each eigenvalue (ties by index)
+  for (int k = tid; k < n; k += BT) {
+    const double v = d[k];
+    int rnk = 0;
+    for (int q = 0; q < n; ++q) rnk += (d[q] < v) || (d[q] == v && q < k);
+    perm[rnk] = k;
+  }
+  __syncthreads();
+
+  // ---------------------------------------------------------------- step 4
+  // X = Phi Z (sorted columns) in the right half: X_a[r, col] = alpha_r z_r, X_b = beta_r z_r
+  double2* XA = A + (int64_t)n * ld;
+  double2* XB = XA + n;
+  for (int t = tid; t < n * n; t += BT) {
+    const int r = t % n, col = t / n;
+    const double z = Z[r + (int64_t)perm[col] * n];
+    XA[r + (int64_t)col * ld] = make_double2(phi[4 * r] * z, phi[4 * r + 1] * z);
+    XB[r + (int64_t)col * ld] = make_double2(phi[4 * r + 2] * z, phi[4 * r + 3] * z);
+  }
+  for (int k = tid; k < n; k += BT) a.eig[tk.eoff + k] = d[perm[k]];
+  __syncthreads();
+  // reflectors backwards: x <- x - w <w,x> - w' [w,x], w' = (-conj(wb), conj(wa))
+  for (int j = n - 3; j >= 0; --j) {
+    const int L = n - 1 - j;
+    for (int i = tid; i < L; i += BT) { swa[i] = A[j + 1 + i + (int64_t)j * ld]; swb[i] = B[j + 1 + i + (int64_t)j * ld]; }
+    __syncthreads();
+    for (int col = warp; col < n; col += BT / 32) {
+      double2* xa = XA + (j + 1) + (int64_t)col * ld;
+      double2* xb = XB + (j + 1) + (int64_t)col * ld;
+      double2 c1 = make_double2(0, 0), c2 = c1;
+      for (int i = lane; i < L; i += 32) {
+        const double2 wa = swa[i], wb = swb[i], va = xa[i], vb = xb[i];
+        cfmac(c1, wa, va); cfmac(c1, wb, vb);
+        cfma(c2, wa, vb); cfma(c2, cneg(wb), va);
+      }
+      c1.x = warp_sum(c1.x); c1.y = warp_sum(c1.y);
+      c2.x = warp_sum(c2.x); c2.y = warp_sum(c2.y);
+      for (int i = lane; i < L; i += 32) {
+        const double2 wa = swa[i], wb = swb[i];
+        double2 va = xa[i], vb = xb[i];
+        // va -= wa c1 - conj(wb) c2 ; vb -= wb c1 + conj(wa) c2
+        double2 ta = make_double2(0, 0), tb = ta;
+        cfma(ta, wa, c1); cfmac(ta, cneg(wb), c2);
+        cfma(tb, wb, c1); cfmac(tb, wa, c2);
+        xa[i] = csub(va, ta);
+        xb[i] = csub(vb, tb);
+      }
+    }
+    __syncthreads();
+  }
+  // output: left half (U; V) = X, right half (-conj(V); conj(U))
+  for (int t = tid; t < n * n; t += BT) {
+    const int r = t % n, col = t / n;
+    const double2 u = XA[r + (int64_t)col * ld], vv = XB[r + (int64_t)col * ld];
+    A[r + (int64_t)col * ld] = u;
+    B[r + (int64_t)col * ld] = vv;
+    XA[r + (int64_t)col * ld] = make_double2(-vv.x, vv.y);
+    XB[r + (int64_t)col * ld] = make_double2(u.x, -u.y);
+  }
+  if (tid == 0) a.info[tk.out_slot] = sflag[0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(BT) k_batched(BatchArgs a) {
+  __shared__ int s_task;
+  double* ws = a.ws + (int64_t)blockIdx.x * a.ws_stride;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int t = s_task;
+    __syncthreads();
+    if (t >= a.count) break;
+    const BatchTask tk = a.tasks[t];
+    if (tk.n > 0) batch_solve_one(tk, a, ws);
+  }
+}
+
+long long batched_ws_stride() {
+  // d (1), e4 (4), offd (1), phi (4), eigenvalues (1), perm (1, ints) -- 12 n -- then Z (n x n)
+  return 12LL * BNMAX + (long long)BNMAX * BNMAX + 64;
+}
+int batched_max_n() { return BNMAX; }
+
+int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
+                   int ctas, int* dev_info, cudaStream_t st) {
+  if (count <= 0) return ZQ_OK;
+  BatchArgs a{};
+  a.tasks = reinterpret_cast<const BatchTask*>(dev_tasks);
+  a.count = count;
+  a.counter = dev_counter;
+  a.D = D;
+  a.eig = eig;
+  a.ws = ws;
+  a.ws_stride = batched_ws_stride();
+  a.info = dev_info;
+  ZQ_CUDA(cudaMemsetAsync(dev_counter, 0, sizeof(int), st));
+  prof_begin(PC_BATCHED, st);
+  k_batched<<<ctas, BT, 0, st>>>(a);
+  prof_end(PC_BATCHED, st);
+  ZQ_LAUNCH_CHECK();
+  return ZQ_OK;
+}
+
+size_t batched_task_bytes() { return sizeof(BatchTask); }
+
+void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot) {
+  BatchTask* t = reinterpret_cast<BatchTask*>(dst);
+  t->off = off; t->eoff = eoff; t->n = n; t->ld = ld; t->out_slot = slot; t->pad = 0;
+}
+
+}  // namespace zq

@@ -71,10 +71,11 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   __shared__ double s_c;
 
   // c_{k-1} = sum of partials (deterministic order)
-  if (k > 0 && tid == 0) {
+  if (k > 0 && tid < 32) {
     double c = 0;
-    for (int i = 0; i < ncp; ++i) c += v.cpart[i];
-    s_c = c;
+    for (int i = tid; i < ncp; i += 32) c += v.cpart[i];
+    c = warp_sum(c);
+    if (tid == 0) s_c = c;
   }
   __syncthreads();
   const R half_c = (k > 0) ? (R)(0.5 * s_c) : (R)0;
@@ -171,17 +172,22 @@ __global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, 
   const int L = n - 1 - j;
   const int tid = threadIdx.x;
   __shared__ double s_sc[5];  // f, first element of w (a.re, a.im, b.re, b.im)
-  if (tid == 0) {
+  double nu = 0.0;
+  if (tid < 32) {
     // combine norm partials: nu = scale * sqrt(ssq)
     double scale = 0.0;
-    for (int i = 0; i < nnp; ++i) scale = fmax(scale, v.npart[2 * i]);
+    for (int i = tid; i < nnp; i += 32) scale = fmax(scale, v.npart[2 * i]);
+    scale = warp_max(scale);
     double ssq = 0.0;
     if (scale > 0.0)
-      for (int i = 0; i < nnp; ++i) {
+      for (int i = tid; i < nnp; i += 32) {
         const double si = v.npart[2 * i];
         if (si > 0.0) { const double q = si / scale; ssq += v.npart[2 * i + 1] * q * q; }
       }
-    const double nu = scale * sqrt(ssq);
+    ssq = warp_sum(ssq);
+    nu = scale * sqrt(ssq);
+  }
+  if (tid == 0) {
     const double qa0 = v.scal[0], qa1 = v.scal[1], qb0 = v.scal[2], qb1 = v.scal[3];
     const double q1 = sqrt(qa0 * qa0 + qa1 * qa1 + qb0 * qb0 + qb1 * qb1);
     double f = 0.0, m[4] = {0.0, 0.0, 0.0, 0.0};
@@ -267,11 +273,16 @@ __global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, 
 template <typename R>
 __global__ void k_dotsum(TridiagView<R> v, int k, int ndp) {
   using Z = cplx<R>;
-  for (int t = threadIdx.x; t < 4 * k; t += blockDim.x) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int t = warp; t < 4 * k; t += nw) {
     const int i = t >> 2, q = t & 3;
-    Z s = czero<Z>();
-    for (int c = 0; c < ndp; ++c) s = cadd(s, v.dpart[((int64_t)c * v.nbmax + i) * 4 + q]);
-    v.dots[t] = s;
+    R sx = 0, sy = 0;
+    for (int c = lane; c < ndp; c += 32) {
+      const Z p = v.dpart[((int64_t)c * v.nbmax + i) * 4 + q];
+      sx += p.x; sy += p.y;
+    }
+    sx = warp_sum(sx); sy = warp_sum(sy);
+    if (lane == 0) v.dots[t] = mk(sx, sy);
   }
 }
 
@@ -393,16 +404,24 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
   __shared__ Z s_dots[4 * 64];
   __shared__ Z s_red[NG][RB][2];
   __shared__ double s_redd[NT / 32];
-  if (!zero_mode && tid < 4 * RB) {
-    const int orow = tid >> 2, ou = tid & 3;
+  __shared__ Z s_half[4 * RB];
+  if (!zero_mode) {
+    const int o = tid & (4 * RB - 1), half = tid >> 7;   // 128 outputs x 2 halves
+    const int orow = o >> 2, ou = o & 3;
     const int lr = blockIdx.x * RB + orow;
-    Z s = czero<Z>();
+    Z s0 = czero<Z>(), s1 = czero<Z>();
     if (r0 + lr < n) {
       const int Rb = lr / T, off = lr % T;
       const int nbm = v.hblk;
-      for (int S = 0; S < nblk; ++S) s = cadd(s, v.hpart[(((int64_t)Rb * nbm + S) * T + off) * 4 + ou]);
+      const Z* base = v.hpart + (((int64_t)Rb * nbm) * T + off) * 4 + ou;
+      const int64_t stride = (int64_t)T * 4;
+      int S = half;
+      for (; S + 2 < nblk; S += 4) { s0 = cadd(s0, base[S * stride]); s1 = cadd(s1, base[(S + 2) * stride]); }
+      for (; S < nblk; S += 2) s0 = cadd(s0, base[S * stride]);
     }
-    s_v[orow][ou] = s;
+    if (half == 1) s_half[o] = cadd(s0, s1);
+    __syncthreads();
+    if (half == 0) s_v[orow][ou] = cadd(cadd(s0, s1), s_half[o]);
   }
   for (int t = tid; t < 4 * k; t += NT) s_dots[t] = v.dots[t];
   __syncthreads();
