@@ -58,6 +58,17 @@ int zq_stedc_device(int n, const double* d, const double* e, double* lam, double
 int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const long long* offs,
                            const long long* eoffs, double* dD, double* deig, void* stream);
 
+/* Single solve of a small matrix (n2 <= 512) in device memory that allocates
+ * nothing: for callers that cannot call cudaMalloc (code running under an
+ * external allocator that owns the device memory, or where allocating device
+ * memory is not allowed). Its scratch is a fixed ~537 KiB array in the
+ * library's device memory, held by every GPU that loads the library until
+ * exit. Larger n2 return -103 (ZQ_ERR_LIMIT). The first call on a device looks
+ * up the array's address (make it before any stream capture). All calls share
+ * the array: calls that overlap on the GPU race. Waits for `stream` and
+ * returns info. No counterpart in the reference. */
+int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig, void* stream);
+
 /* Panel width of the blocked tridiagonalisation (the reference hard-codes
  * nb = 20 at zquatev.cc:64). Valid range 1..64; default 32. */
 int zq_set_block_size(int nb);

@@ -21,6 +21,7 @@ SIGNATURES = {
     "zquatev_values_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
     "zq_stedc_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),
     "zquatev_batched_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "zquatev_device_noalloc": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
     "zq_profile_enable": (_c_int, [_c_int]),
     "zq_profile_read": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "zq_profile_reset": (_c_int, []),

@@ -40,6 +40,7 @@ void set_last_error(cudaError_t e, const char* what, const char* file, int line)
 }
 const char* last_error_message() { return g_last_error.c_str(); }
 static void set_msg(const char* m) { g_last_error = m; }
+void set_error_message(const char* msg) { g_last_error = msg; }
 
 // ----------------------------------------------------------------------------
 // per-kernel-class event timing

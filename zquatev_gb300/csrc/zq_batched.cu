@@ -22,6 +22,8 @@
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
+#include <mutex>
+
 namespace zq {
 
 constexpr int BT = 256;        // threads per CTA
@@ -372,4 +374,82 @@ void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, 
   t->off = off; t->eoff = eoff; t->n = n; t->ld = ld; t->out_slot = slot; t->pad = 0;
 }
 
+// ----------------------------------------------------------------------------
+// Single small solve that allocates nothing.
+//
+// For callers that cannot call cudaMalloc: code that runs under an external
+// allocator which owns the device memory budget (a framework's caching
+// allocator, a pre-sized memory pool), or in a context where allocating
+// device memory is not allowed. The solver's scratch (one per-CTA workspace of
+// the batched kernel) lives in the file-scope device array below, of fixed
+// size; the caller passes D and eig as for zquatev_device.
+//
+// Limits and behaviour:
+//   * n2 <= 2 * BNMAX = 512 (quaternion order 256); larger sizes are rejected
+//     with ZQ_ERR_LIMIT before anything is launched.
+//   * The scratch is ~537 KiB (NOALLOC_SCRATCH_DOUBLES doubles) and is held by
+//     every GPU that loads this library until the process exits.
+//   * The first call on a device looks up the array's device address with
+//     cudaGetSymbolAddress (once per device, with that device current); make
+//     that first call before any stream capture.
+//   * Every call shares the one array, which keeps the previous call's
+//     contents; the kernel writes every scratch word before it reads it, so
+//     nothing has to be cleared. Calls whose work overlaps on the GPU (on
+//     different streams, or from different host threads) race on the array.
+//   * The call waits for its stream and returns info (0, or > 0 when the
+//     tridiagonal QL did not converge).
+// ----------------------------------------------------------------------------
+constexpr long long NOALLOC_SCRATCH_DOUBLES = 12LL * BNMAX + (long long)BNMAX * BNMAX + 64 + 8;
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+__global__ void __launch_bounds__(BT) k_solve_small_noalloc(BatchTask tk, double2* D, double* eig, double* scratch,
+                                                            int* info) {
+  BatchArgs a{};
+  a.D = D;
+  a.eig = eig;
+  a.ws = scratch;
+  a.info = info;
+  batch_solve_one(tk, a, scratch);
+}
+
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_dev[64];  // device address of g_noalloc_scratch, per device
+
 }  // namespace zq
+
+extern "C" int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig, void* stream) {
+  using namespace zq;
+  if (n2 < 0 || (n2 & 1)) return ZQ_ERR_N2;
+  if (n2 == 0) return ZQ_OK;
+  if (!dD) return ZQ_ERR_D;
+  if (ld2 < n2) return ZQ_ERR_LD;
+  if (!deig) return ZQ_ERR_EIG;
+  if (n2 > 2 * BNMAX) {
+    set_error_message("zquatev_device_noalloc: n2 above its fixed limit of 512");
+    return ZQ_ERR_LIMIT;
+  }
+  int dev = 0;
+  ZQ_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return ZQ_ERR_ARG;
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_dev[dev]) {
+      void* p = nullptr;
+      ZQ_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      g_noalloc_dev[dev] = reinterpret_cast<double*>(p);
+    }
+    scratch = g_noalloc_dev[dev];
+  }
+  const long long stride = 12LL * BNMAX + (long long)BNMAX * BNMAX + 64;
+  int* info_dev = reinterpret_cast<int*>(scratch + stride);
+  BatchTask tk{};
+  tk.off = 0; tk.eoff = 0; tk.n = n2 / 2; tk.ld = ld2; tk.out_slot = 0;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  k_solve_small_noalloc<<<1, BT, 0, st>>>(tk, reinterpret_cast<double2*>(dD), deig, scratch, info_dev);
+  ZQ_CUDA(cudaGetLastError());
+  int info = 0;
+  ZQ_CUDA(cudaMemcpyAsync(&info, info_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ZQ_CUDA(cudaStreamSynchronize(st));
+  return info;
+}

@@ -121,6 +121,7 @@ enum Status : int {
 #define ZQ_LAUNCH_CHECK() ZQ_CUDA(cudaGetLastError())
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line);
+void set_error_message(const char* msg);
 const char* last_error_message();
 
 // Optional per-kernel-class timing with CUDA events recorded on the launching
