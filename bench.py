@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-check", action="store_true")
     p.add_argument("--cpu-sample-n2", type=int, default=1024)
+    p.add_argument("--profile-n2", type=int, default=0,
+                   help="profiling case: run --reps solves of this size through the host C ABI and exit")
+    p.add_argument("--reps", type=int, default=1)
     return p.parse_args()
 
 
@@ -225,9 +228,29 @@ def run_reference(args, rank, world):
 
 
 # --------------------------------------------------------------- GPU arm
+def profile_case(n2: int, reps: int) -> None:
+    """Plain solves of one random matrix (the command ncu captures are taken on)."""
+    from zquatev_gb300 import _lib, build, inputs, solver
+
+    if not build.up_to_date():
+        build.build()
+    n = n2 // 2
+    d = inputs.random_matrix(n, 3)
+    for _ in range(reps):
+        out = d.copy(order="F")
+        eig = np.zeros(n2)
+        rc = solver.zquatev(n2, out, n2, eig)
+        if rc != 0:
+            raise SystemExit(f"zquatev_c rc={rc}: {_lib.last_error()}")
+    print(f"profile case n2={n2} x{reps}: ok")
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
+    if args.profile_n2:
+        profile_case(args.profile_n2, args.reps)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
