@@ -58,6 +58,17 @@ int zq_stedc_device(int n, const double* d, const double* e, double* lam, double
 int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const long long* offs,
                            const long long* eoffs, double* dD, double* deig, void* stream);
 
+/* Mixed-precision solve with iterative refinement, same arguments and output
+ * as zquatev_device (device memory, ordered after `stream`, synchronises once
+ * per refinement step to read the correction size). An FP32 decomposition is
+ * refined to FP64 accuracy by Ogita-Aishima iterations on the quaternion form;
+ * mode 0 computes the refinement products in native FP64, mode 1 with
+ * Ozaki-sliced bf16 tensor-core products accumulated exactly. The reference
+ * has only the FP64 path (zquatev.cc:42-100). */
+int zquatev_refined_device(int n2, double* dD, int ld2, double* deig, void* stream, int mode);
+/* Iterations and final max |E| of the last refined solve on this device. */
+int zq_refine_stats(int* iters, double* last_correction);
+
 /* Single solve of a small matrix (n2 <= 512) in device memory that allocates
  * nothing: for callers that cannot call cudaMalloc (code running under an
  * external allocator that owns the device memory, or where allocating device

@@ -22,6 +22,8 @@ SIGNATURES = {
     "zq_stedc_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _c_int, _vp]),
     "zquatev_batched_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "zquatev_device_noalloc": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
+    "zquatev_refined_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp, _c_int]),
+    "zq_refine_stats": (_c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
     "zq_profile_enable": (_c_int, [_c_int]),
     "zq_profile_read": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "zq_profile_reset": (_c_int, []),

@@ -239,7 +239,7 @@ static int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* dei
     ZQ_CUDA(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
     double2* X = dD + (int64_t)n * ldd;  // right half as workspace (as the reference does)
     prof_begin(PC_FORMQ, c->st2);
-    if (int rc = form_q(dD, ldd, n, phi, X, ldd, nbq, fq_ws, c->st2)) return rc;
+    if (int rc = form_q<double>(dD, ldd, n, phi, X, ldd, nbq, fq_ws, c->st2)) return rc;
     prof_end(PC_FORMQ, c->st2);
     ZQ_CUDA(cudaEventRecord(c->ev_join, c->st2));
     double* Z = nullptr;
@@ -249,7 +249,7 @@ static int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* dei
     tm.mark("stedc", c->st);
     ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_join, 0));
     tm.mark("formq-wait", c->st);
-    if (int rc = apply_z(X, ldd, Z, n, n, dD, ldd, desc1, c->st)) return rc;
+    if (int rc = apply_z<double>(X, ldd, Z, n, n, dD, ldd, desc1, c->st)) return rc;
     tm.mark("apply_z", c->st);
     if (int rc = symmetry_fill(dD, ldd, n, c->st)) return rc;
     tm.mark("symfill", c->st);
@@ -306,6 +306,69 @@ static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors) 
   cudaFreeAsync(dD, c->st);
   cudaStreamSynchronize(c->st);
   return rc;
+}
+
+// ----------------------------------------------------------------------------
+// refined (mixed-precision) path
+// ----------------------------------------------------------------------------
+struct RefineBuffers {
+  void* dev = nullptr;
+  size_t bytes = 0;
+  int last_iters = 0;
+  double last_emax = 0.0;
+};
+static RefineBuffers g_refine[64];
+size_t ozaki_workspace_bytes(int n);
+
+static int ensure_plan(Context* c, int n) {
+  if (c->dc_n == n) return ZQ_OK;
+  DcPlan probe;
+  probe.build(n);
+  Layout L = layout_for(n, 64, g_nbq, probe.num_nodes(), probe.num_descs());
+  if (int rc = ensure_ws(c, L.total)) return rc;
+  c->dc = probe;
+  char* base = reinterpret_cast<char*>(c->ws);
+  char* p = base + L.tri + L.small;
+  double* dcws = reinterpret_cast<double*>(p); p += L.dc + L.fq;
+  DcNode* nodes = reinterpret_cast<DcNode*>(p); p += L.nodes;
+  if (int rc = c->dc.upload(dcws, nodes, reinterpret_cast<DgemmDesc*>(p), c->st)) return rc;
+  c->dc_n = n;
+  return ZQ_OK;
+}
+
+static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cudaStream_t st, int mode) {
+  if (int rc = ensure_plan(c, n)) return rc;
+  RefineBuffers& rb = g_refine[c->device];
+  const size_t need = refine_workspace_bytes(n, g_nbq) + (mode == 1 ? ozaki_workspace_bytes(n) : 0) + 4096;
+  if (rb.bytes < need) {
+    if (rb.dev) { cudaStreamSynchronize(c->st); cudaFree(rb.dev); rb.dev = nullptr; rb.bytes = 0; }
+    ZQ_CUDA(cudaMalloc(&rb.dev, need));
+    rb.bytes = need;
+  }
+  Layout L = layout_for(n, 64, g_nbq, c->dc.num_nodes(), c->dc.num_descs());
+  DgemmDesc* desc1 = reinterpret_cast<DgemmDesc*>(reinterpret_cast<char*>(c->ws) + L.tri + L.small + L.dc + L.fq + L.nodes) +
+                     c->dc.num_descs();
+  RefineArgs ra{};
+  ra.dD = dD; ra.ldd = ldd; ra.n = n; ra.deig = deig;
+  ra.ws = reinterpret_cast<char*>(rb.dev) + 4096;
+  const size_t rws = refine_workspace_bytes(n, g_nbq);
+  ra.ows = (mode == 1) ? reinterpret_cast<char*>(ra.ws) + ((rws + 255) & ~(size_t)255) : nullptr;
+  ra.ows_bytes = (mode == 1) ? ozaki_workspace_bytes(n) : 0;
+  ra.dc = &c->dc;
+  ra.fdesc = reinterpret_cast<DgemmDescT<float>*>(desc1);
+  ra.nb = nb_for(n); ra.nbq = g_nbq; ra.mode = mode;
+  ra.max_iter = 4;
+  ra.tol = 1e-8;
+  if (const char* s = getenv("ZQ_REFINE_MAXIT")) ra.max_iter = atoi(s);
+  ra.st = c->st;
+  ZQ_CUDA(cudaEventRecord(c->ev_fork, st));
+  ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
+  if (int rc = refined_solve(ra)) return rc;
+  rb.last_iters = ra.iters;
+  rb.last_emax = ra.last_emax;
+  ZQ_CUDA(cudaEventRecord(c->ev_join, c->st));
+  ZQ_CUDA(cudaStreamWaitEvent(st, c->ev_join, 0));
+  return ZQ_OK;
 }
 
 // ----------------------------------------------------------------------------
@@ -460,6 +523,24 @@ int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const lon
   if (count == 0) return ZQ_OK;
   return batched_solve(count, n2s, ld2s, offs, eoffs, reinterpret_cast<double2*>(dD), deig,
                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zquatev_refined_device(int n2, double* dD, int ld2, double* deig, void* stream, int mode) {
+  if (int rc = check_args(n2, dD, ld2, deig)) return rc;
+  if (n2 == 0) return ZQ_OK;
+  if (mode < 0 || mode > 1) { set_msg("mode must be 0 (FP64 products) or 1 (Ozaki tensor-core products)"); return ZQ_ERR_ARG; }
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  return refined_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, reinterpret_cast<cudaStream_t>(stream), mode);
+}
+
+int zq_refine_stats(int* iters, double* last_correction) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ZQ_ERR_CUDA;
+  if (iters) *iters = g_refine[dev].last_iters;
+  if (last_correction) *last_correction = g_refine[dev].last_emax;
+  return ZQ_OK;
 }
 
 int zq_profile_enable(int mask) {

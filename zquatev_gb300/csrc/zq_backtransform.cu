@@ -57,24 +57,26 @@ int phase_reduce(const double* e, int n, double* offd, double* phi, cudaStream_t
 }
 
 // X = [diag(alpha); diag(beta)]
-__global__ void k_init_x(double2* X, int64_t ldx, int n, const double* phi) {
+template <typename Z>
+__global__ void k_init_x(Z* X, int64_t ldx, int n, const double* phi) {
   const int64_t total = (int64_t)2 * n * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(t % (2 * n));
     const int c = (int)(t / (2 * n));
-    double2 v = make_double2(0.0, 0.0);
-    if (r == c) v = make_double2(phi[4 * c], phi[4 * c + 1]);
-    else if (r == n + c) v = make_double2(phi[4 * c + 2], phi[4 * c + 3]);
+    Z v = czero<Z>();
+    if (r == c) { v.x = phi[4 * c]; v.y = phi[4 * c + 1]; }
+    else if (r == n + c) { v.x = phi[4 * c + 2]; v.y = phi[4 * c + 3]; }
     X[r + (int64_t)c * ldx] = v;
   }
 }
 
 // pack the block's reflectors: Wa[r, i] = A(p+1+r, p+i) for r >= i, else 0 (same for B)
-__global__ void k_pack_w(const double2* M, int64_t ldm, int n, int p, int kb, int L, double2* Wa, double2* Wb) {
+template <typename Z>
+__global__ void k_pack_w(const Z* M, int64_t ldm, int n, int p, int kb, int L, Z* Wa, Z* Wb) {
   const int64_t total = (int64_t)L * kb;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(t % L), i = (int)(t / L);
-    double2 va = make_double2(0.0, 0.0), vb = va;
+    Z va = czero<Z>(), vb = va;
     if (r >= i) {
       const int64_t o = (p + 1 + r) + (int64_t)(p + i) * ldm;
       va = M[o];
@@ -90,18 +92,19 @@ __global__ void k_pack_w(const double2* M, int64_t ldm, int n, int p, int kb, in
 // One CTA of 1024 threads: thread (i, g) sums the l = i+g, i+g+16, ... terms of
 // column k; the 16 partials of each row are reduced in shared memory.
 constexpr int BT_G = 16;
-__global__ void __launch_bounds__(1024) k_build_t(const double2* G1, const double2* G2, int kb, double2* Ta, double2* Tb) {
+template <typename Z>
+__global__ void __launch_bounds__(1024) k_build_t(const Z* G1, const Z* G2, int kb, Z* Ta, Z* Tb) {
   const int tid = threadIdx.x;
   const int i = tid & 63, g = tid >> 6;
-  __shared__ double2 red[BT_G][64][2];
-  for (int t = tid; t < kb * kb; t += blockDim.x) { Ta[t] = make_double2(0.0, 0.0); Tb[t] = make_double2(0.0, 0.0); }
+  __shared__ Z red[BT_G][64][2];
+  for (int t = tid; t < kb * kb; t += blockDim.x) { Ta[t] = czero<Z>(); Tb[t] = czero<Z>(); }
   __syncthreads();
   for (int k = 0; k < kb; ++k) {
-    double2 sa = make_double2(0.0, 0.0), sb = sa;
+    Z sa = czero<Z>(), sb = sa;
     if (i < k) {
       for (int l = i + g; l < k; l += BT_G) {
-        const double2 ta = Ta[i + l * kb], tb = Tb[i + l * kb];
-        const double2 g1 = G1[l + k * kb], g2 = G2[l + k * kb];
+        const Z ta = Ta[i + l * kb], tb = Tb[i + l * kb];
+        const Z g1 = G1[l + k * kb], g2 = G2[l + k * kb];
         // q(ta, tb) q(g1, g2) = q(ta g1 - conj(tb) g2, tb g1 + conj(ta) g2)
         cfma(sa, ta, g1); cfmac(sa, cneg(tb), g2);
         cfma(sb, tb, g1); cfmac(sb, ta, g2);
@@ -112,13 +115,15 @@ __global__ void __launch_bounds__(1024) k_build_t(const double2* G1, const doubl
     __syncthreads();
     if (g == 0) {
       if (i < k) {
-        double2 ta = make_double2(0.0, 0.0), tb = ta;
+        Z ta = czero<Z>(), tb = ta;
         for (int q = 0; q < BT_G; ++q) { ta = cadd(ta, red[q][i][0]); tb = cadd(tb, red[q][i][1]); }
         Ta[i + k * kb] = cneg(ta);
         Tb[i + k * kb] = cneg(tb);
       } else if (i == k) {
-        Ta[k + k * kb] = make_double2(1.0, 0.0);
-        Tb[k + k * kb] = make_double2(0.0, 0.0);
+        Z one = czero<Z>();
+        one.x = 1;
+        Ta[k + k * kb] = one;
+        Tb[k + k * kb] = czero<Z>();
       }
     }
     __syncthreads();
@@ -133,103 +138,114 @@ size_t form_q_workspace_bytes(int n, int nbq) {
   return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n + (size_t)fq_pcap(n, nbq)) + 256;
 }
 
-int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, int64_t ldx, int nbq, void* ws,
+template <typename R>
+int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, int64_t ldx, int nbq, void* ws,
            cudaStream_t st) {
+  using Z = cplx<R>;
+  using Args = ZgemmArgsT<R>;
   if (n <= 0) return ZQ_OK;
-  k_init_x<<<ceil_div(2 * n * n, 256) > 4096 ? 4096 : ceil_div(2 * n * n, 256), 256, 0, st>>>(X, ldx, n, phi);
+  k_init_x<Z><<<ceil_div(2 * n * n, 256) > 4096 ? 4096 : ceil_div(2 * n * n, 256), 256, 0, st>>>(X, ldx, n, phi);
   ZQ_LAUNCH_CHECK();
   const int nref = n - 2;  // reflectors exist for columns 0..n-3
   if (nref <= 0) return ZQ_OK;
-  double2* p = reinterpret_cast<double2*>(ws);
-  double2* Wa = p; p += (size_t)n * nbq;
-  double2* Wb = p; p += (size_t)n * nbq;
-  double2* G1 = p; p += (size_t)nbq * nbq;
-  double2* G2 = p; p += (size_t)nbq * nbq;
-  double2* Ta = p; p += (size_t)nbq * nbq;
-  double2* Tb = p; p += (size_t)nbq * nbq;
-  double2* C1e = p; p += (size_t)nbq * n;
-  double2* C1o = p; p += (size_t)nbq * n;
-  double2* C2e = p; p += (size_t)nbq * n;
-  double2* C2o = p; p += (size_t)nbq * n;
-  double2* Pk = p;
+  Z* p = reinterpret_cast<Z*>(ws);
+  Z* Wa = p; p += (size_t)n * nbq;
+  Z* Wb = p; p += (size_t)n * nbq;
+  Z* G1 = p; p += (size_t)nbq * nbq;
+  Z* G2 = p; p += (size_t)nbq * nbq;
+  Z* Ta = p; p += (size_t)nbq * nbq;
+  Z* Tb = p; p += (size_t)nbq * nbq;
+  Z* C1e = p; p += (size_t)nbq * n;
+  Z* C1o = p; p += (size_t)nbq * n;
+  Z* C2e = p; p += (size_t)nbq * n;
+  Z* C2o = p; p += (size_t)nbq * n;
+  Z* Pk = p;
   const int64_t pcap = fq_pcap(n, nbq);
-  double2* Xa = X;
-  double2* Xb = X + n;
+  Z* Xa = X;
+  Z* Xb = X + n;
+  Z one = czero<Z>(), zero = czero<Z>(), mone = czero<Z>();
+  one.x = 1; mone.x = -1;
   const int nblocks = ceil_div(nref, nbq);
   for (int bi = nblocks - 1; bi >= 0; --bi) {
     const int pb = bi * nbq;
     const int kb = (nbq < nref - pb) ? nbq : (nref - pb);
     const int L = n - 1 - pb;
-    k_pack_w<<<ceil_div(L * kb, 256) > 2048 ? 2048 : ceil_div(L * kb, 256), 256, 0, st>>>(M, ldm, n, pb, kb, L, Wa, Wb);
+    k_pack_w<Z><<<ceil_div(L * kb, 256) > 2048 ? 2048 : ceil_div(L * kb, 256), 256, 0, st>>>(M, ldm, n, pb, kb, L, Wa, Wb);
     ZQ_LAUNCH_CHECK();
-    ZgemmArgs g{};
+    Args g{};
     g.P = Pk; g.pcap = pcap;
     // G1 = Wa^H Wa + Wb^H Wb ; G2 = Wa^T Wb - Wb^T Wa   (kb x kb, inner L)
-    g = ZgemmArgs{};
+    g = Args{};
     g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = kb; g.k1 = L; g.k2 = L;
     g.A1 = Wa; g.lda1 = L; g.B1 = Wa; g.ldb1 = L;
     g.A2 = Wb; g.lda2 = L; g.B2 = Wb; g.ldb2 = L;
-    g.s2 = 1.0; g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+    g.s2 = (R)1; g.alpha = one; g.beta = zero;
     g.C = G1; g.ldc = kb;
     if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
-    g.A1 = Wa; g.B1 = Wb; g.A2 = Wb; g.B2 = Wa; g.s2 = -1.0; g.C = G2;
+    g.A1 = Wa; g.B1 = Wb; g.A2 = Wb; g.B2 = Wa; g.s2 = (R)-1; g.C = G2;
     if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
-    k_build_t<<<1, 1024, 0, st>>>(G1, G2, kb, Ta, Tb);
+    k_build_t<Z><<<1, 1024, 0, st>>>(G1, G2, kb, Ta, Tb);
     ZQ_LAUNCH_CHECK();
     // C1e = Wa^H Xa_sub + Wb^H Xb_sub ; C1o = Wa^T Xb_sub - Wb^T Xa_sub   (kb x L)
-    double2* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
-    double2* Xbs = Xb + (pb + 1) + (int64_t)(pb + 1) * ldx;
-    g = ZgemmArgs{};
+    Z* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
+    Z* Xbs = Xb + (pb + 1) + (int64_t)(pb + 1) * ldx;
+    g = Args{};
     g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = L; g.k1 = L; g.k2 = L;
     g.A1 = Wa; g.lda1 = L; g.B1 = Xas; g.ldb1 = ldx;
     g.A2 = Wb; g.lda2 = L; g.B2 = Xbs; g.ldb2 = ldx;
-    g.s2 = 1.0; g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+    g.s2 = (R)1; g.alpha = one; g.beta = zero;
     g.C = C1e; g.ldc = kb;
     if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
-    g.A1 = Wa; g.B1 = Xbs; g.A2 = Wb; g.B2 = Xas; g.s2 = -1.0; g.C = C1o;
+    g.A1 = Wa; g.B1 = Xbs; g.A2 = Wb; g.B2 = Xas; g.s2 = (R)-1; g.C = C1o;
     if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
     // C2e = Ta C1e - conj(Tb) C1o ; C2o = Tb C1e + conj(Ta) C1o   (kb x L)
-    g = ZgemmArgs{};
+    g = Args{};
     g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = L; g.k1 = kb; g.k2 = kb;
     g.A1 = Ta; g.lda1 = kb; g.B1 = C1e; g.ldb1 = kb;
     g.A2 = Tb; g.lda2 = kb; g.B2 = C1o; g.ldb2 = kb;
-    g.s2 = -1.0; g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+    g.s2 = (R)-1; g.alpha = one; g.beta = zero;
     g.C = C2e; g.ldc = kb;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
-    g.A1 = Tb; g.A2 = Ta; g.s2 = 1.0; g.C = C2o;
+    g.A1 = Tb; g.A2 = Ta; g.s2 = (R)1; g.C = C2o;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
     // Xa_sub -= Wa C2e - conj(Wb) C2o ; Xb_sub -= Wb C2e + conj(Wa) C2o   (L x L)
-    g = ZgemmArgs{};
+    g = Args{};
     g.P = Pk; g.pcap = pcap;
     g.m = L; g.n = L; g.k1 = kb; g.k2 = kb;
     g.A1 = Wa; g.lda1 = L; g.B1 = C2e; g.ldb1 = kb;
     g.A2 = Wb; g.lda2 = L; g.B2 = C2o; g.ldb2 = kb;
-    g.s2 = -1.0; g.alpha = make_double2(-1.0, 0.0); g.beta = make_double2(1.0, 0.0);
+    g.s2 = (R)-1; g.alpha = mone; g.beta = one;
     g.C = Xas; g.ldc = ldx;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
-    g.A1 = Wb; g.A2 = Wa; g.s2 = 1.0; g.C = Xbs;
+    g.A1 = Wb; g.A2 = Wa; g.s2 = (R)1; g.C = Xbs;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
   }
   return ZQ_OK;
 }
 
-int apply_z(const double2* X, int64_t ldx, const double* Z, int64_t ldz, int n, double2* out, int64_t ldo,
-            DgemmDesc* dev_desc, cudaStream_t st) {
+template <typename R>
+int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<R>* out, int64_t ldo,
+            DgemmDescT<R>* dev_desc, cudaStream_t st) {
   if (n <= 0) return ZQ_OK;
-  DgemmDesc d{};
-  d.A = reinterpret_cast<const double*>(X); d.lda = 2 * ldx;
+  DgemmDescT<R> d{};
+  d.A = reinterpret_cast<const R*>(X); d.lda = 2 * ldx;
   d.B = Z; d.ldb = ldz;
-  d.C = reinterpret_cast<double*>(out); d.ldc = 2 * ldo;
+  d.C = reinterpret_cast<R*>(out); d.ldc = 2 * ldo;
   d.m = 4 * n; d.n = n; d.k = n;
-  d.alpha = 1.0; d.beta = 0.0;
+  d.alpha = 1; d.beta = 0;
   prof_begin(PC_APPLYZ, st);
-  const int rc = dgemm_grouped(&d, 1, dev_desc, st);
+  const int rc = dgemm_grouped<R>(&d, 1, dev_desc, st);
   prof_end(PC_APPLYZ, st);
   return rc;
 }
+
+template int form_q<double>(const cplx<double>*, int64_t, int, const double*, cplx<double>*, int64_t, int, void*, cudaStream_t);
+template int form_q<float>(const cplx<float>*, int64_t, int, const double*, cplx<float>*, int64_t, int, void*, cudaStream_t);
+template int apply_z<double>(const cplx<double>*, int64_t, const double*, int64_t, int, cplx<double>*, int64_t, DgemmDescT<double>*, cudaStream_t);
+template int apply_z<float>(const cplx<float>*, int64_t, const float*, int64_t, int, cplx<float>*, int64_t, DgemmDescT<float>*, cudaStream_t);
 
 __global__ void k_symfill(double2* D, int64_t ld, int n) {
   const int64_t total = (int64_t)n * n;

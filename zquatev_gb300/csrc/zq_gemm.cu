@@ -27,29 +27,30 @@ constexpr int GK = 8;    // k per stage (complex)
 constexpr int GKR = 16;  // k per stage (real)
 constexpr int GNT = 256;
 
-template <int OP>
-__device__ __forceinline__ double2 load_op(const double2* X, int64_t ldx, int r, int c) {
+template <int OP, typename Z>
+__device__ __forceinline__ Z load_op(const Z* X, int64_t ldx, int r, int c) {
   // element (r, c) of op(X)
   if (OP == OP_N) return X[r + (int64_t)c * ldx];
-  if (OP == OP_R) { double2 v = X[r + (int64_t)c * ldx]; v.y = -v.y; return v; }
+  if (OP == OP_R) { Z v = X[r + (int64_t)c * ldx]; v.y = -v.y; return v; }
   if (OP == OP_T) return X[c + (int64_t)r * ldx];
-  double2 v = X[c + (int64_t)r * ldx]; v.y = -v.y; return v;  // OP_C
+  Z v = X[c + (int64_t)r * ldx]; v.y = -v.y; return v;  // OP_C
 }
 
-template <int OPA1, int OPB1, int OPA2, int OPB2>
-__global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
-  __shared__ double sA[3][GK][GT];
-  __shared__ double sB[3][GK][GT];
+template <typename R, int OPA1, int OPB1, int OPA2, int OPB2>
+__global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgsT<R> g) {
+  using Z = cplx<R>;
+  __shared__ R sA[3][GK][GT];
+  __shared__ R sB[3][GK][GT];
   const int tid = threadIdx.x;
   const int tr = tid & 15, tc = tid >> 4;
   const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
   const int split = blockIdx.z;
-  const double2* A1 = g.A1;
-  const double2* B1 = g.B1;
-  const double2* A2 = g.A2;
-  const double2* B2 = g.B2;
-  double2* C = g.C;
-  double t1[4][4], t2[4][4], t3[4][4];
+  const Z* A1 = g.A1;
+  const Z* B1 = g.B1;
+  const Z* A2 = g.A2;
+  const Z* B2 = g.B2;
+  Z* C = g.C;
+  R t1[4][4], t2[4][4], t3[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -58,7 +59,7 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
   const int nseg = (A2 != nullptr) ? 2 : 1;
   for (int seg = 0; seg < nseg; ++seg) {
     const int K = seg == 0 ? g.k1 : g.k2;
-    const double sgn = seg == 0 ? 1.0 : g.s2;
+    const R sgn = seg == 0 ? (R)1 : g.s2;
     // this split's share of the segment, in whole GK steps
     const int steps = (K + GK - 1) / GK;
     const int sb = (int)(((int64_t)steps * split) / gridDim.z), se = (int)(((int64_t)steps * (split + 1)) / gridDim.z);
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
         int r, kk;
         const bool a_kfast = (seg == 0 ? (OPA1 == OP_T || OPA1 == OP_C) : (OPA2 == OP_T || OPA2 == OP_C));
         if (a_kfast) { kk = e % GK; r = e / GK; } else { r = e % GT; kk = e / GT; }
-        double2 va = make_double2(0.0, 0.0);
+        Z va = czero<Z>();
         if (i0 + r < g.m && k0 + kk < K) {
           va = seg == 0 ? load_op<OPA1>(A1, g.lda1, i0 + r, k0 + kk) : load_op<OPA2>(A2, g.lda2, i0 + r, k0 + kk);
           va.x *= sgn; va.y *= sgn;
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
         int c;
         const bool b_kfast = (seg == 0 ? (OPB1 == OP_N || OPB1 == OP_R) : (OPB2 == OP_N || OPB2 == OP_R));
         if (b_kfast) { kk = e % GK; c = e / GK; } else { c = e % GT; kk = e / GT; }
-        double2 vb = make_double2(0.0, 0.0);
+        Z vb = czero<Z>();
         if (j0 + c < g.n && k0 + kk < K)
           vb = seg == 0 ? load_op<OPB1>(B1, g.ldb1, k0 + kk, j0 + c) : load_op<OPB2>(B2, g.ldb2, k0 + kk, j0 + c);
         sB[0][kk][c] = vb.x; sB[1][kk][c] = vb.y; sB[2][kk][c] = vb.x + vb.y;
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < GK; ++kk) {
-        double ar[4], ai[4], as[4], br[4], bi[4], bs[4];
+        R ar[4], ai[4], as[4], br[4], bi[4], bs[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           ar[q] = sA[0][kk][tr + 16 * q]; ai[q] = sA[1][kk][tr + 16 * q]; as[q] = sA[2][kk][tr + 16 * q];
@@ -105,7 +106,7 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
   }
   if (gridDim.z > 1) {
     // raw partial sums; k_zsplit_reduce applies alpha/beta
-    double2* P = g.P + (int64_t)split * g.m * g.n;
+    Z* P = g.P + (int64_t)split * g.m * g.n;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
       const int i = i0 + tr + 16 * a;
@@ -114,13 +115,13 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
       for (int b = 0; b < 4; ++b) {
         const int j = j0 + tc + 16 * b;
         if (j >= g.n) continue;
-        P[i + (int64_t)j * g.m] = make_double2(t1[a][b] - t2[a][b], t3[a][b] - t1[a][b] - t2[a][b]);
+        P[i + (int64_t)j * g.m] = mk(t1[a][b] - t2[a][b], t3[a][b] - t1[a][b] - t2[a][b]);
       }
     }
     return;
   }
-  const double2 al = g.alpha, be = g.beta;
-  const bool use_beta = (be.x != 0.0 || be.y != 0.0);
+  const Z al = g.alpha, be = g.beta;
+  const bool use_beta = (be.x != (R)0 || be.y != (R)0);
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     const int i = i0 + tr + 16 * a;
@@ -129,12 +130,12 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
     for (int b = 0; b < 4; ++b) {
       const int j = j0 + tc + 16 * b;
       if (j >= g.n) continue;
-      const double re = t1[a][b] - t2[a][b];
-      const double im = t3[a][b] - t1[a][b] - t2[a][b];
-      double2 out = make_double2(al.x * re - al.y * im, al.x * im + al.y * re);
+      const R re = t1[a][b] - t2[a][b];
+      const R im = t3[a][b] - t1[a][b] - t2[a][b];
+      Z out = mk(al.x * re - al.y * im, al.x * im + al.y * re);
       const int64_t o = i + (int64_t)j * g.ldc;
       if (use_beta) {
-        const double2 c = C[o];
+        const Z c = C[o];
         out.x += be.x * c.x - be.y * c.y;
         out.y += be.x * c.y + be.y * c.x;
       }
@@ -143,20 +144,22 @@ __global__ void __launch_bounds__(GNT) k_zgemm(ZgemmArgs g) {
   }
 }
 
-__global__ void k_zsplit_reduce(ZgemmArgs g, int splits) {
+template <typename R>
+__global__ void k_zsplit_reduce(ZgemmArgsT<R> g, int splits) {
+  using Z = cplx<R>;
   const int64_t total = (int64_t)g.m * g.n;
-  const bool use_beta = (g.beta.x != 0.0 || g.beta.y != 0.0);
+  const bool use_beta = (g.beta.x != (R)0 || g.beta.y != (R)0);
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    double re = 0.0, im = 0.0;
+    R re = 0, im = 0;
     for (int s = 0; s < splits; ++s) {
-      const double2 p = g.P[t + (int64_t)s * total];
+      const Z p = g.P[t + (int64_t)s * total];
       re += p.x; im += p.y;
     }
     const int i = (int)(t % g.m), j = (int)(t / g.m);
-    double2 out = make_double2(g.alpha.x * re - g.alpha.y * im, g.alpha.x * im + g.alpha.y * re);
+    Z out = mk(g.alpha.x * re - g.alpha.y * im, g.alpha.x * im + g.alpha.y * re);
     const int64_t o = i + (int64_t)j * g.ldc;
     if (use_beta) {
-      const double2 c = g.C[o];
+      const Z c = g.C[o];
       out.x += g.beta.x * c.x - g.beta.y * c.y;
       out.y += g.beta.x * c.y + g.beta.y * c.x;
     }
@@ -166,7 +169,8 @@ __global__ void k_zsplit_reduce(ZgemmArgs g, int splits) {
 
 // Split the K range over enough CTAs to fill the GPU when the output is small
 // (e.g. the 64 x L products of the Q formation); partials go to g.P.
-static int choose_splits(const ZgemmArgs& g) {
+template <typename R>
+static int choose_splits(const ZgemmArgsT<R>& g) {
   if (!g.P || g.pcap <= 0) return 1;
   const int tiles = ceil_div(g.m, GT) * ceil_div(g.n, GT);
   const int ksteps = ceil_div(g.k1, GK) + (g.A2 ? ceil_div(g.k2, GK) : 0);
@@ -175,28 +179,29 @@ static int choose_splits(const ZgemmArgs& g) {
   return s;
 }
 
-template <int OPA1, int OPB1, int OPA2, int OPB2>
-int zgemm_launch(const ZgemmArgs& g, int batch, cudaStream_t st) {
+template <typename R, int OPA1, int OPB1, int OPA2, int OPB2>
+int zgemm_launch(const ZgemmArgsT<R>& g, int batch, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0) return ZQ_OK;
   (void)batch;
   const int splits = choose_splits(g);
   dim3 grid(ceil_div(g.m, GT), ceil_div(g.n, GT), splits);
   prof_begin(PC_FORMQ_GEMM, st);
-  k_zgemm<OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
+  k_zgemm<R, OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
   prof_end(PC_FORMQ_GEMM, st);
   ZQ_LAUNCH_CHECK();
   if (splits > 1) {
     const int64_t total = (int64_t)g.m * g.n;
     const int blocks = (int)((total + 255) / 256 > 4096 ? 4096 : (total + 255) / 256);
-    k_zsplit_reduce<<<blocks, 256, 0, st>>>(g, splits);
+    k_zsplit_reduce<R><<<blocks, 256, 0, st>>>(g, splits);
     ZQ_LAUNCH_CHECK();
   }
   return ZQ_OK;
 }
 
-int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, int batch, cudaStream_t st) {
+template <typename R>
+int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgsT<R>& g, int batch, cudaStream_t st) {
 #define ZQ_Z(a, b, c, d) \
-  if (opa1 == a && opb1 == b && opa2 == c && opb2 == d) return zgemm_launch<a, b, c, d>(g, batch, st);
+  if (opa1 == a && opb1 == b && opa2 == c && opb2 == d) return zgemm_launch<R, a, b, c, d>(g, batch, st);
   // the combinations used by the solver
   ZQ_Z(OP_C, OP_N, OP_C, OP_N)   // Wa^H Xa + Wb^H Xb
   ZQ_Z(OP_T, OP_N, OP_T, OP_N)   // Wa^T Xb - Wb^T Xa
@@ -205,16 +210,20 @@ int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, int batch,
   ZQ_Z(OP_C, OP_N, OP_N, OP_N)
   ZQ_Z(OP_N, OP_C, OP_N, OP_N)
   ZQ_Z(OP_T, OP_N, OP_N, OP_N)
+  ZQ_Z(OP_N, OP_R, OP_N, OP_N)   // A conj(B)
 #undef ZQ_Z
   return ZQ_ERR_ARG;
 }
+template int zgemm<double>(int, int, int, int, const ZgemmArgsT<double>&, int, cudaStream_t);
+template int zgemm<float>(int, int, int, int, const ZgemmArgsT<float>&, int, cudaStream_t);
 
 // ----------------------------------------------------------------------------
 // real grouped GEMM
 // ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDesc* __restrict__ descs, int count) {
-  __shared__ double sA[GKR][GT];
-  __shared__ double sB[GKR][GT + 1];
+template <typename R>
+__global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDescT<R>* __restrict__ descs, int count) {
+  __shared__ R sA[GKR][GT];
+  __shared__ R sB[GKR][GT + 1];
   // locate descriptor (linear search over prefix offsets; count is small)
   const int t = blockIdx.x;
   int gi = 0;
@@ -226,29 +235,29 @@ __global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDesc* __restri
     }
     gi = lo;
   }
-  const DgemmDesc d = descs[gi];
+  const DgemmDescT<R> d = descs[gi];
   const int local = t - d.tile0;
   const int mt = (d.m + GT - 1) / GT;
   const int i0 = (local % mt) * GT, j0 = (local / mt) * GT;
   const int tid = threadIdx.x;
   const int tr = tid & 15, tc = tid >> 4;
-  double acc[4][4];
+  R acc[4][4];
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0;
   for (int k0 = 0; k0 < d.k; k0 += GKR) {
     __syncthreads();
     for (int e = tid; e < GKR * GT; e += GNT) {
       int r, kk;
       if (d.ta) { kk = e % GKR; r = e / GKR; } else { r = e % GT; kk = e / GT; }
-      double va = 0.0;
+      R va = 0;
       if (i0 + r < d.m && k0 + kk < d.k)
         va = d.ta ? d.A[(k0 + kk) + (int64_t)(i0 + r) * d.lda] : d.A[(i0 + r) + (int64_t)(k0 + kk) * d.lda];
       sA[kk][r] = va;
       int c;
       if (!d.tb) { kk = e % GKR; c = e / GKR; } else { c = e % GT; kk = e / GT; }
-      double vb = 0.0;
+      R vb = 0;
       if (j0 + c < d.n && k0 + kk < d.k)
         vb = d.tb ? d.B[(j0 + c) + (int64_t)(k0 + kk) * d.ldb] : d.B[(k0 + kk) + (int64_t)(j0 + c) * d.ldb];
       sB[kk][c] = vb;
@@ -256,7 +265,7 @@ __global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDesc* __restri
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GKR; ++kk) {
-      double a[4], b[4];
+      R a[4], b[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) { a[q] = sA[kk][tr + 16 * q]; b[q] = sB[kk][tc + 16 * q]; }
 #pragma unroll
@@ -274,8 +283,8 @@ __global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDesc* __restri
       const int j = j0 + tc + 16 * y;
       if (j >= d.n) continue;
       const int64_t o = i + (int64_t)j * d.ldc;
-      double out = d.alpha * acc[x][y];
-      if (d.beta != 0.0) out += d.beta * d.C[o];
+      R out = d.alpha * acc[x][y];
+      if (d.beta != (R)0) out += d.beta * d.C[o];
       d.C[o] = out;
     }
   }
@@ -283,26 +292,29 @@ __global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDesc* __restri
 
 void k_dgemm_grouped_launch(const DgemmDesc* dev_descs, int count, int tiles, cudaStream_t st) {
   if (tiles <= 0 || count <= 0) return;
-  k_dgemm_grouped<<<tiles, GNT, 0, st>>>(dev_descs, count);
+  k_dgemm_grouped<double><<<tiles, GNT, 0, st>>>(dev_descs, count);
 }
 
 int dgemm_tiles(int m, int n) { return ceil_div(m, GT) * ceil_div(n, GT); }
 
-int dgemm_grouped(DgemmDesc* host_descs, int count, DgemmDesc* dev_descs, cudaStream_t st) {
+template <typename R>
+int dgemm_grouped(DgemmDescT<R>* host_descs, int count, DgemmDescT<R>* dev_descs, cudaStream_t st) {
   int tiles = 0;
   int used = 0;
   for (int i = 0; i < count; ++i) {
-    DgemmDesc& d = host_descs[i];
+    DgemmDescT<R>& d = host_descs[i];
     if (d.m <= 0 || d.n <= 0) continue;
     d.tile0 = tiles;
     tiles += ceil_div(d.m, GT) * ceil_div(d.n, GT);
     host_descs[used++] = d;
   }
   if (used == 0) return ZQ_OK;
-  ZQ_CUDA(cudaMemcpyAsync(dev_descs, host_descs, sizeof(DgemmDesc) * used, cudaMemcpyHostToDevice, st));
-  k_dgemm_grouped<<<tiles, GNT, 0, st>>>(dev_descs, used);
+  ZQ_CUDA(cudaMemcpyAsync(dev_descs, host_descs, sizeof(DgemmDescT<R>) * used, cudaMemcpyHostToDevice, st));
+  k_dgemm_grouped<R><<<tiles, GNT, 0, st>>>(dev_descs, used);
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;
 }
+template int dgemm_grouped<double>(DgemmDescT<double>*, int, DgemmDescT<double>*, cudaStream_t);
+template int dgemm_grouped<float>(DgemmDescT<float>*, int, DgemmDescT<float>*, cudaStream_t);
 
 }  // namespace zq

@@ -43,29 +43,35 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st);
 // ---------------------------------------------------------------------- GEMM
 enum { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };
 
-struct ZgemmArgs {
+template <typename R>
+struct ZgemmArgsT {
   int m, n, k1, k2;
-  const double2* A1; int64_t lda1;
-  const double2* B1; int64_t ldb1;
-  const double2* A2; int64_t lda2;   // null: single segment
-  const double2* B2; int64_t ldb2;
-  double s2;
-  double2 alpha, beta;
-  double2* C; int64_t ldc;
-  double2* P; int64_t pcap;          // optional split-K partial buffer (complex elements)
+  const cplx<R>* A1; int64_t lda1;
+  const cplx<R>* B1; int64_t ldb1;
+  const cplx<R>* A2; int64_t lda2;   // null: single segment
+  const cplx<R>* B2; int64_t ldb2;
+  R s2;
+  cplx<R> alpha, beta;
+  cplx<R>* C; int64_t ldc;
+  cplx<R>* P; int64_t pcap;          // optional split-K partial buffer (complex elements)
 };
-int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, int batch, cudaStream_t st);
+using ZgemmArgs = ZgemmArgsT<double>;
+template <typename R>
+int zgemm(int opa1, int opb1, int opa2, int opb2, const ZgemmArgsT<R>& g, int batch, cudaStream_t st);
 
-struct DgemmDesc {
-  const double* A; const double* B; double* C;
+template <typename R>
+struct DgemmDescT {
+  const R* A; const R* B; R* C;
   int64_t lda, ldb, ldc;
   int64_t off_a, off_b, off_c;  // plan-time offsets (bound to pointers before upload)
   int m, n, k;
   int ta, tb;
   int tile0;
-  double alpha, beta;
+  R alpha, beta;
 };
-int dgemm_grouped(DgemmDesc* host_descs, int count, DgemmDesc* dev_descs, cudaStream_t st);
+using DgemmDesc = DgemmDescT<double>;
+template <typename R>
+int dgemm_grouped(DgemmDescT<R>* host_descs, int count, DgemmDescT<R>* dev_descs, cudaStream_t st);
 void k_dgemm_grouped_launch(const DgemmDesc* dev_descs, int count, int tiles, cudaStream_t st);
 int dgemm_tiles(int m, int n);
 
@@ -110,13 +116,30 @@ struct DcPlan {
 // real off-diagonal |e_k| and unit quaternions phi_k = (alpha_k, beta_k)
 int phase_reduce(const double* e, int n, double* offd, double* phi, cudaStream_t st);
 // X = [diag(alpha); diag(beta)] (2n x n complex, ld), then Q X by blocked reflectors
-int form_q(const double2* M, int64_t ldm, int n, const double* phi, double2* X, int64_t ldx,
+template <typename R>
+int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, int64_t ldx,
            int nbq, void* ws, cudaStream_t st);
 size_t form_q_workspace_bytes(int n, int nbq);
 // out (2n x n complex, ldo) = X (2n x n complex, ldx) * Z (n x n real, ldz)
-int apply_z(const double2* X, int64_t ldx, const double* Z, int64_t ldz, int n, double2* out, int64_t ldo,
-            DgemmDesc* dev_desc, cudaStream_t st);
+template <typename R>
+int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<R>* out, int64_t ldo,
+            DgemmDescT<R>* dev_desc, cudaStream_t st);
 // right half of the n2 x n2 output from the left half (U; V)
 int symmetry_fill(double2* D, int64_t ld, int n, cudaStream_t st);
+
+// ------------------------------------------------------ refined (mixed) path
+struct RefineArgs {
+  double2* dD; int64_t ldd; int n; double* deig;
+  void* ws;                    // refine_workspace_bytes(n, nbq)
+  void* ows; size_t ows_bytes; // accurate-product workspace (mode 1)
+  DcPlan* dc;                  // uploaded plan for n
+  DgemmDescT<float>* fdesc;    // one device descriptor slot
+  int nb, nbq, mode, max_iter;
+  double tol;
+  cudaStream_t st;
+  int iters; double last_emax;  // outputs
+};
+size_t refine_workspace_bytes(int n, int nbq);
+int refined_solve(RefineArgs& ra);
 
 }  // namespace zq
