@@ -69,6 +69,14 @@ int zquatev_refined_device(int n2, double* dD, int ld2, double* deig, void* stre
 /* Iterations and final max |E| of the last refined solve on this device. */
 int zq_refine_stats(int* iters, double* last_correction);
 
+/* FP64-accurate complex product C = op(A) op(B) (m x n, inner k; op 0 = N,
+ * 1 = T, 2 = conjugate transpose, 3 = conjugate) on the bf16 tensor cores with
+ * Ozaki slicing and exact accumulation (the engine of the refinement). All
+ * pointers are device memory (interleaved complex, column-major); allocates
+ * its scratch with cudaMallocAsync on `stream`. No reference counterpart. */
+int zq_zgemm_accurate(int opa, int opb, int m, int n, int k, const double* A, int lda, const double* B, int ldb,
+                      double* C, int ldc, void* stream);
+
 /* Single solve of a small matrix (n2 <= 512) in device memory that allocates
  * nothing: for callers that cannot call cudaMalloc (code running under an
  * external allocator that owns the device memory, or where allocating device
@@ -90,7 +98,8 @@ int zq_get_block_size(void);
  * bracketed launch). Classes: 0 quaternion hemv, 1 trailing update, 2 panel
  * column kernels, 3 Q-formation GEMMs, 4 back-transform GEMM, 5 tridiagonal
  * eigensolver, 6 whole tridiagonalisation, 7 whole Q formation, 8 batched
- * kernel. No reference counterpart. */
+ * kernel, 9 Ozaki tensor-core product, 10 whole refinement. No reference
+ * counterpart. */
 int zq_profile_enable(int mask);
 int zq_profile_read(int cls, double* total_ms, long long* launches);
 int zq_profile_reset(void);

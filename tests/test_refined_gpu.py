@@ -39,3 +39,33 @@ def test_refined_random(gpu, n, mode):
     assert metrics.orthonormality(out) <= TOL
     assert metrics.structure_exact(out, n)
     assert np.all(np.diff(eig[:n]) >= 0)
+
+
+@pytest.mark.parametrize("opa,opb", [(2, 0), (1, 0), (0, 0), (0, 3)])
+def test_accurate_zgemm(gpu, opa, opb):
+    """The Ozaki tensor-core product agrees with an extended-precision product to ~1e-15 relative."""
+    import torch
+
+    rng = np.random.default_rng(opa * 10 + opb)
+    m, n, k = 70, 50, 300
+    ash = (k, m) if opa in (1, 2) else (m, k)
+    bsh = (n, k) if opb in (1, 2) else (k, n)
+    a = rng.standard_normal(ash) + 1j * rng.standard_normal(ash)
+    b = rng.standard_normal(bsh) + 1j * rng.standard_normal(bsh)
+    a[3] *= 1e-5  # rows of very different scale
+    def op(x, o):
+        return {0: x, 1: x.T, 2: x.conj().T, 3: x.conj()}[o]
+    al = op(a.astype(np.clongdouble), opa)
+    bl = op(b.astype(np.clongdouble), opb)
+    exact = al @ bl
+    da = torch.from_numpy(np.ascontiguousarray(a.T)).cuda()
+    db = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()
+    dc = torch.zeros((n, m), dtype=torch.complex128, device="cuda")
+    rc = gpu.zq_zgemm_accurate(opa, opb, m, n, k, da.data_ptr(), ash[0], db.data_ptr(), bsh[0], dc.data_ptr(), m,
+                               torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert rc == 0, _lib.last_error()
+    c = dc.cpu().numpy().T
+    scale = np.abs(op(a, opa)) @ np.abs(op(b, opb))
+    err = np.abs(c - exact.astype(np.complex128)) / scale
+    assert err.max() < 2e-15

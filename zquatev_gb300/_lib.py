@@ -24,6 +24,7 @@ SIGNATURES = {
     "zquatev_device_noalloc": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
     "zquatev_refined_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp, _c_int]),
     "zq_refine_stats": (_c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    "zq_zgemm_accurate": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _c_int, _vp, _c_int, _vp]),
     "zq_profile_enable": (_c_int, [_c_int]),
     "zq_profile_read": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "zq_profile_reset": (_c_int, []),
@@ -72,7 +73,7 @@ def check(rc: int, what: str) -> int:
 
 
 PROFILE_CLASSES = {"hemv": 0, "trail": 1, "panel": 2, "formq_gemm": 3, "apply_z": 4, "stedc": 5,
-                   "tridiag": 6, "formq": 7, "batched": 8}
+                   "tridiag": 6, "formq": 7, "batched": 8, "ozaki": 9, "refine": 10}
 
 
 def profile_read(name: str) -> tuple[float, int]:

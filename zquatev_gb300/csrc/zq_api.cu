@@ -358,7 +358,7 @@ static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* d
   ra.fdesc = reinterpret_cast<DgemmDescT<float>*>(desc1);
   ra.nb = nb_for(n); ra.nbq = g_nbq; ra.mode = mode;
   ra.max_iter = 4;
-  ra.tol = 1e-8;
+  ra.tol = 1e-7;   // the update squares the error: |E| <= 1e-7 leaves ~1e-14
   if (const char* s = getenv("ZQ_REFINE_MAXIT")) ra.max_iter = atoi(s);
   ra.st = c->st;
   ZQ_CUDA(cudaEventRecord(c->ev_fork, st));

@@ -129,7 +129,7 @@ const char* last_error_message();
 // brackets one launch; totals are read back after a synchronisation.
 enum ProfClass : int {
   PC_HEMV = 0, PC_TRAIL = 1, PC_PANEL = 2, PC_FORMQ_GEMM = 3, PC_APPLYZ = 4,
-  PC_STEDC = 5, PC_TRIDIAG = 6, PC_FORMQ = 7, PC_BATCHED = 8, PC_COUNT = 9
+  PC_STEDC = 5, PC_TRIDIAG = 6, PC_FORMQ = 7, PC_BATCHED = 8, PC_OZAKI = 9, PC_REFINE = 10, PC_COUNT = 11
 };
 void prof_begin(int cls, cudaStream_t st);
 void prof_end(int cls, cudaStream_t st);

@@ -142,4 +142,16 @@ struct RefineArgs {
 size_t refine_workspace_bytes(int n, int nbq);
 int refined_solve(RefineArgs& ra);
 
+// Ozaki-sliced FP64-accurate complex product (zq_ozaki.cu)
+struct OzOpts {
+  int slices;      // bf16 slices per operand (7 bits each), 2..8
+  int structured;  // 0 general; +1 Hermitian / -1 antisymmetric square output (lower tiles computed)
+  int reuse_a;     // 1: the A operand is the same as in the previous call (slices kept)
+};
+int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st,
+                const OzOpts& opt);
+size_t ozaki_workspace_bytes(int n);
+// upper triangle of a square structured matrix from its lower triangle (sym +1 Hermitian, -1 antisymmetric)
+int structured_fill(double2* C, int64_t ldc, int n, int sym, cudaStream_t st);
+
 }  // namespace zq

@@ -1,14 +1,487 @@
-// Ozaki-sliced complex products on the tensor cores (placeholder: FP64).
+// FP64-accurate complex matrix products on the bf16 tensor cores (Ozaki
+// scheme I, error-free slicing), used by the refinement products G = X^H X,
+// H X and S = X^H (H X) of zq_refine.cu.
+//
+// Scheme (Ozaki, Ogita, Oishi & Rump, Numer. Algorithms 59 (2012) 95-118;
+// the bf16 / FP32-accumulate variant with exact chunked accumulation):
+//   * the complex product C = op(A1) op(B1) + s2 op(A2) op(B2) is written as two
+//     real products with the K dimension concatenated:
+//       Re C = Ahat . Bre,  Im C = Ahat . Bim,
+//       Ahat = [ar1 | ai1 | s2 ar2 | s2 ai2],  Bre = [br1 | -bi1 | br2 | -bi2],
+//       Bim  = [bi1 | br1 | bi2 | br2];
+//   * every row of Ahat is scaled by a power of two sigma_i >= its max |entry|
+//     (every column of B by tau_j) and cut into S slices of BETA = 7 bits:
+//     integers in [-128, 128], exact in bf16;
+//   * slice products are integers <= 2^14; FP32 accumulation of up to 256 of
+//     them is exact (< 2^22), so the tensor-core accumulator is emptied into an
+//     int32 accumulator every 256 terms (exact), and each (level, super-chunk)
+//     writes its int32 result; level l = t + u collects the slice pairs (t, u)
+//     with t + u = l, l < S (the triangular truncation);
+//   * the combine kernel forms C = sigma_i tau_j sum_l 2^(-BETA (l + 2)) I_l in
+//     FP64.
+// With S = 7 the dropped terms are below 2^-49 of sigma_i tau_j per product,
+// i.e. FP64-level accuracy for the refinement's sums.
+//
+// The product kernel is a bf16 mma.sync (m16n8k16) tiled GEMM: 64x64 CTA
+// tile, four 32x32 warp tiles computing the real and imaginary outputs from one
+// staged A tile and two B tiles, cp.async double buffering.
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
+#include <cuda_bf16.h>
+#include <vector>
+
 namespace zq {
 
-size_t ozaki_workspace_bytes(int n) { (void)n; return 256; }
+constexpr int OZ_BETA = 7;
+constexpr int OZ_SMAX = 8;              // most slices per operand (56 bits)
+constexpr int OZ_CHUNK = 256;            // exact FP32 accumulation length
+constexpr int OZ_SUPER = 64 * 1024;      // terms per int32 partial (64 * 1024 * 2^14 < 2^31)
+constexpr int OZ_TM = 64, OZ_TN = 64, OZ_TK = 64;
+constexpr int OZ_LDS = OZ_TK + 8;        // padded shared row (bf16), 144 bytes
+constexpr int OZ_THREADS = 128;
 
-int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st) {
-  (void)ws; (void)ws_bytes;
-  return zgemm<double>(opa1, opb1, opa2, opb2, g, 1, st);
+// element (r, c) of op(X)
+__device__ __forceinline__ double2 oz_op(const double2* X, int64_t ld, int op, int r, int c) {
+  double2 v;
+  if (op == OP_N || op == OP_R) v = X[r + (int64_t)c * ld];
+  else v = X[c + (int64_t)r * ld];
+  if (op == OP_R || op == OP_C) v.y = -v.y;
+  return v;
+}
+
+struct OzSide {
+  const double2* X1; int64_t ld1; int op1; int K1;
+  const double2* X2; int64_t ld2; int op2; int K2;
+  double s2;
+};
+
+// value of Ahat[i][k'] (rows of op(A)) or of Bre/Bim[j][k'] (columns of op(B))
+__device__ __forceinline__ void oz_entry(const OzSide& s, bool is_a, int idx, int kp, double& v_re_form, double& v_im_form) {
+  int seg = 0, k = kp;
+  if (k >= 2 * s.K1) { seg = 1; k -= 2 * s.K1; }
+  const int K = seg ? s.K2 : s.K1;
+  if (k >= 2 * K) { v_re_form = 0.0; v_im_form = 0.0; return; }  // padding
+  const bool imag_half = k >= K;
+  const int kk = imag_half ? k - K : k;
+  double2 x;
+  if (is_a) x = seg ? oz_op(s.X2, s.ld2, s.op2, idx, kk) : oz_op(s.X1, s.ld1, s.op1, idx, kk);
+  else x = seg ? oz_op(s.X2, s.ld2, s.op2, kk, idx) : oz_op(s.X1, s.ld1, s.op1, kk, idx);
+  if (is_a) {
+    const double sg = seg ? s.s2 : 1.0;
+    v_re_form = sg * (imag_half ? x.y : x.x);
+    v_im_form = v_re_form;
+  } else {
+    v_re_form = imag_half ? -x.y : x.x;  // Bre = [br | -bi]
+    v_im_form = imag_half ? x.x : x.y;   // Bim = [bi | br]
+  }
+}
+
+// exponent e with 2^e >= max |entry| of row/column idx (e = -1100 for a zero row)
+__global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict__ exps) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= count) return;
+  double mx = 0.0;
+  for (int kp = lane; kp < Kp; kp += 32) {
+    double a, b;
+    oz_entry(s, is_a, warp, kp, a, b);
+    mx = fmax(mx, fabs(a));
+  }
+  mx = warp_max(mx);
+  if (lane == 0) {
+    int e = -1100;
+    if (mx > 0.0) {
+      int ex;
+      const double f = frexp(mx, &ex);  // mx = f 2^ex, f in [0.5, 1)
+      e = ex;                           // 2^ex > mx
+      (void)f;
+    }
+    exps[warp] = e;
+  }
+}
+
+// S slices of one operand: out[t][idx][kp] (bf16), idx < padded count (zero rows above count).
+// The slices are the base-128 digits of floor(|v| / 2^e * 2^(7 S)) (integer
+// arithmetic on the 53-bit significand), with the sign of v: exact truncation.
+__global__ void k_oz_slice(OzSide s, bool is_a, int count, int count_pad, int Kp, const int* __restrict__ exps,
+                           int nsl, __nv_bfloat16* __restrict__ out_re, __nv_bfloat16* __restrict__ out_im,
+                           int64_t slice_stride) {
+  const int64_t total = (int64_t)count_pad * Kp;
+  const int F = OZ_BETA * nsl;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int idx = (int)(t / Kp), kp = (int)(t % Kp);
+    double v[2] = {0.0, 0.0};
+    int e = 0;
+    if (idx < count) {
+      oz_entry(s, is_a, idx, kp, v[0], v[1]);
+      e = exps[idx];
+    }
+    unsigned long long V[2];
+    bool neg[2];
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(v[c]);
+      neg[c] = (bits >> 63) != 0;
+      const int ex = (int)((bits >> 52) & 0x7ff);
+      unsigned long long mant = bits & ((1ull << 52) - 1);
+      int ebits = ex;
+      if (ex == 0) ebits = 1; else mant |= (1ull << 52);
+      // |v| = mant * 2^(ebits - 1075);  V = floor(|v| 2^(F - e))
+      const int sh = ebits - 1075 - e + F;
+      if (mant == 0 || e < -1000) V[c] = 0;
+      else if (sh >= 0) V[c] = (sh >= 64) ? 0 : (mant << sh);
+      else V[c] = (-sh >= 64) ? 0 : (mant >> (-sh));
+    }
+    for (int q = 0; q < nsl; ++q) {
+      const int shift = F - OZ_BETA * (q + 1);
+      const int dr = (int)((V[0] >> shift) & 127), di = (int)((V[1] >> shift) & 127);
+      out_re[q * slice_stride + t] = __int2bfloat16_rn(neg[0] ? -dr : dr);
+      if (out_im) out_im[q * slice_stride + t] = __int2bfloat16_rn(neg[1] ? -di : di);
+    }
+  }
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void* smem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(s));
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+struct OzGemmArgs {
+  const __nv_bfloat16* A;    // [S][mp][Kp]
+  const __nv_bfloat16* Bre;  // [S][np][Kp]
+  const __nv_bfloat16* Bim;
+  int64_t sa, sb;            // slice strides (elements)
+  int mp, np, Kp;
+  int* out;                  // [nsc][2][np][mp]
+  int nsc;
+  int nsl;                   // slices per operand
+  int lower;                 // 1: only tiles with I >= J (square structured outputs)
+};
+
+// One CTA per 64x64 tile; loops over all levels and super-chunks.
+__global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzGemmArgs g) {
+  extern __shared__ __align__(16) unsigned char oz_smem[];
+  __nv_bfloat16* sm = reinterpret_cast<__nv_bfloat16*>(oz_smem);
+  // stage layout: A [64][LDS], Bre [64][LDS], Bim [64][LDS]; two stages
+  const int stage_elems = 3 * OZ_TM * OZ_LDS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 1, wn = warp & 1;
+  int bi = blockIdx.x, bj = blockIdx.y;
+  if (g.lower) {
+    const int t = blockIdx.x;
+    int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((I + 1) * (I + 2) / 2 <= t) ++I;
+    while (I * (I + 1) / 2 > t) --I;
+    bi = I; bj = t - I * (I + 1) / 2;
+  }
+  const int i0 = bi * OZ_TM, j0 = bj * OZ_TN;
+  const int64_t mp = g.mp, np = g.np;
+  int sc = 0;
+  for (int lev = 0; lev < g.nsl; ++lev) {
+    const int64_t total_k = (int64_t)(lev + 1) * g.Kp;
+    for (int64_t kbeg = 0; kbeg < total_k; kbeg += OZ_SUPER) {
+      const int64_t kend = (kbeg + OZ_SUPER < total_k) ? kbeg + OZ_SUPER : total_k;
+      const int ntiles = (int)((kend - kbeg) / OZ_TK);
+      float fr[2][4][4], fi[2][4][4];
+      int ir[2][4][4], ii[2][4][4];
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) { fr[a][b][c] = 0.f; fi[a][b][c] = 0.f; ir[a][b][c] = 0; ii[a][b][c] = 0; }
+
+      auto load_stage = [&](int st, int tile) {
+        const int64_t kg = kbeg + (int64_t)tile * OZ_TK;
+        const int t = (int)(kg / g.Kp);
+        const int kk = (int)(kg % g.Kp);
+        const int u = lev - t;
+        const __nv_bfloat16* Ab = g.A + t * g.sa + (int64_t)i0 * g.Kp + kk;
+        const __nv_bfloat16* Brb = g.Bre + u * g.sb + (int64_t)j0 * g.Kp + kk;
+        const __nv_bfloat16* Bib = g.Bim + u * g.sb + (int64_t)j0 * g.Kp + kk;
+        __nv_bfloat16* s = sm + st * stage_elems;
+        // 64 rows x 8 chunks of 16 B per operand
+        for (int c = tid; c < 64 * 8; c += OZ_THREADS) {
+          const int row = c >> 3, ch = c & 7;
+          cp_async16(s + row * OZ_LDS + ch * 8, Ab + (int64_t)row * g.Kp + ch * 8);
+          cp_async16(s + OZ_TM * OZ_LDS + row * OZ_LDS + ch * 8, Brb + (int64_t)row * g.Kp + ch * 8);
+          cp_async16(s + 2 * OZ_TM * OZ_LDS + row * OZ_LDS + ch * 8, Bib + (int64_t)row * g.Kp + ch * 8);
+        }
+        cp_async_commit();
+      };
+
+      load_stage(0, 0);
+      for (int tile = 0; tile < ntiles; ++tile) {
+        const int st = tile & 1;
+        if (tile + 1 < ntiles) {
+          load_stage(st ^ 1, tile + 1);
+          cp_async_wait_one();
+        } else {
+          cp_async_wait_all();
+        }
+        __syncthreads();
+        const __nv_bfloat16* sA = sm + st * stage_elems;
+        const __nv_bfloat16* sBr = sA + OZ_TM * OZ_LDS;
+        const __nv_bfloat16* sBi = sBr + OZ_TM * OZ_LDS;
+#pragma unroll
+        for (int ks = 0; ks < OZ_TK / 16; ++ks) {
+          unsigned af[2][4];
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt) {
+            const int q = lane >> 3;
+            const int row = wm * 32 + mt * 16 + (q & 1) * 8 + (lane & 7);
+            const int col = ks * 16 + (q >> 1) * 8;
+            ldsm_x4(af[mt], sA + row * OZ_LDS + col);
+          }
+          unsigned br[4][2], bi[4][2];
+#pragma unroll
+          for (int pr = 0; pr < 2; ++pr) {
+            const int q = lane >> 3;
+            const int row = wn * 32 + pr * 16 + (q >> 1) * 8 + (lane & 7);
+            const int col = ks * 16 + (q & 1) * 8;
+            unsigned r[4];
+            ldsm_x4(r, sBr + row * OZ_LDS + col);
+            br[2 * pr][0] = r[0]; br[2 * pr][1] = r[1]; br[2 * pr + 1][0] = r[2]; br[2 * pr + 1][1] = r[3];
+            ldsm_x4(r, sBi + row * OZ_LDS + col);
+            bi[2 * pr][0] = r[0]; bi[2 * pr][1] = r[1]; bi[2 * pr + 1][0] = r[2]; bi[2 * pr + 1][1] = r[3];
+          }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+              mma_bf16(fr[mt][nt], af[mt], br[nt][0], br[nt][1]);
+              mma_bf16(fi[mt][nt], af[mt], bi[nt][0], bi[nt][1]);
+            }
+        }
+        __syncthreads();
+        // empty the FP32 accumulators every OZ_CHUNK terms (exact integers)
+        if (((tile + 1) * OZ_TK) % OZ_CHUNK == 0 || tile + 1 == ntiles) {
+#pragma unroll
+          for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                ir[a][b][c] += __float2int_rz(fr[a][b][c]); fr[a][b][c] = 0.f;
+                ii[a][b][c] += __float2int_rz(fi[a][b][c]); fi[a][b][c] = 0.f;
+              }
+        }
+      }
+      // store this (level, super-chunk) partial: out[sc][ri][j][i]
+      int* o_re = g.out + ((int64_t)sc * 2 + 0) * np * mp;
+      int* o_im = g.out + ((int64_t)sc * 2 + 1) * np * mp;
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+          const int r = i0 + wm * 32 + mt * 16 + (lane >> 2);
+          const int c = j0 + wn * 32 + nt * 8 + 2 * (lane & 3);
+          o_re[(int64_t)c * mp + r] = ir[mt][nt][0];
+          o_re[(int64_t)(c + 1) * mp + r] = ir[mt][nt][1];
+          o_re[(int64_t)c * mp + r + 8] = ir[mt][nt][2];
+          o_re[(int64_t)(c + 1) * mp + r + 8] = ir[mt][nt][3];
+          o_im[(int64_t)c * mp + r] = ii[mt][nt][0];
+          o_im[(int64_t)(c + 1) * mp + r] = ii[mt][nt][1];
+          o_im[(int64_t)c * mp + r + 8] = ii[mt][nt][2];
+          o_im[(int64_t)(c + 1) * mp + r + 8] = ii[mt][nt][3];
+        }
+      ++sc;
+    }
+  }
+}
+
+// C = alpha * sigma_i tau_j sum_sc 2^(-BETA (lev_sc + 2)) (I_re + i I_im) + beta * C
+__global__ void k_oz_combine(const int* __restrict__ parts, int nsc, const int* __restrict__ sc_lev, int mp, int np,
+                             const int* __restrict__ ea, const int* __restrict__ eb, int m, int n, double2 alpha,
+                             double2 beta, double2* __restrict__ C, int64_t ldc, int lower) {
+  const int64_t total = (int64_t)m * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % m), j = (int)(t / m);
+    if (lower && (i >> 6) < (j >> 6)) continue;  // tile not computed
+    double re = 0.0, im = 0.0;
+    const int e0 = ea[i], e1 = eb[j];
+    if (e0 > -1000 && e1 > -1000) {
+      for (int q = 0; q < nsc; ++q) {
+        const int64_t o = (int64_t)j * mp + i;
+        const double sc = ldexp(1.0, e0 + e1 - OZ_BETA * (sc_lev[q] + 2));
+        re += sc * (double)parts[((int64_t)q * 2 + 0) * np * mp + o];
+        im += sc * (double)parts[((int64_t)q * 2 + 1) * np * mp + o];
+      }
+    }
+    double2 out = make_double2(alpha.x * re - alpha.y * im, alpha.x * im + alpha.y * re);
+    const int64_t oc = i + (int64_t)j * ldc;
+    if (beta.x != 0.0 || beta.y != 0.0) {
+      const double2 c = C[oc];
+      out.x += beta.x * c.x - beta.y * c.y;
+      out.y += beta.x * c.y + beta.y * c.x;
+    }
+    C[oc] = out;
+  }
+}
+
+static int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
+
+static int oz_nsc(int Kp, int nsl, std::vector<int>* lev) {
+  int nsc = 0;
+  for (int l = 0; l < nsl; ++l) {
+    const int64_t total = (int64_t)(l + 1) * Kp;
+    for (int64_t k = 0; k < total; k += OZ_SUPER) { if (lev) lev->push_back(l); ++nsc; }
+  }
+  return nsc;
+}
+
+// workspace for products with m, n <= 2 * nq and Kp <= 4 * nq + 64
+size_t ozaki_workspace_bytes(int nq) {
+  const int64_t mp = rup(2 * (int64_t)nq, 64), np = rup(2 * (int64_t)nq, 64), Kp = rup(4 * (int64_t)nq, 64);
+  const int nsc = oz_nsc((int)Kp, OZ_SMAX, nullptr);
+  size_t b = 0;
+  b += sizeof(__nv_bfloat16) * (size_t)OZ_SMAX * mp * Kp;       // A slices
+  b += sizeof(__nv_bfloat16) * (size_t)OZ_SMAX * np * Kp * 2;   // B slices (re / im forms)
+  b += sizeof(int) * (size_t)nsc * 2 * mp * np;              // int32 partials
+  b += sizeof(int) * (size_t)(mp + np + 64);
+  return b + 8 * 256;
+}
+
+// structured square outputs: fill the upper triangle from the lower one
+// (sym = +1 Hermitian, -1 complex antisymmetric); diagonal 64-tiles averaged
+__global__ void k_oz_symfill(double2* __restrict__ C, int64_t ldc, int n, int sym) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n), j = (int)(t / n);
+    if (i < j) continue;
+    const int64_t oij = i + (int64_t)j * ldc, oji = j + (int64_t)i * ldc;
+    double2 a = C[oij];
+    if ((i >> 6) == (j >> 6)) {
+      const double2 b = C[oji];
+      if (sym > 0) a = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
+      else a = make_double2(0.5 * (a.x - b.x), 0.5 * (a.y - b.y));
+    }
+    if (i == j) {
+      if (sym > 0) a.y = 0.0; else a = make_double2(0.0, 0.0);
+    }
+    C[oij] = a;
+    C[oji] = (sym > 0) ? make_double2(a.x, -a.y) : make_double2(-a.x, -a.y);
+  }
+}
+
+int structured_fill(double2* C, int64_t ldc, int n, int sym, cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  const int64_t total = (int64_t)n * n;
+  const int blocks = (int)((total + 255) / 256 > 16384 ? 16384 : (total + 255) / 256);
+  k_oz_symfill<<<blocks, 256, 0, st>>>(C, ldc, n, sym);
+  ZQ_LAUNCH_CHECK();
+  return ZQ_OK;
+}
+
+int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st,
+                const OzOpts& opt) {
+  const int m = g.m, n = g.n;
+  if (m <= 0 || n <= 0) return ZQ_OK;
+  const int nsl = (opt.slices >= 2 && opt.slices <= OZ_SMAX) ? opt.slices : 7;
+  const bool two = g.A2 != nullptr;
+  OzSide a{}, b{};
+  a.X1 = g.A1; a.ld1 = g.lda1; a.op1 = opa1; a.K1 = g.k1;
+  a.X2 = two ? g.A2 : nullptr; a.ld2 = g.lda2; a.op2 = opa2; a.K2 = two ? g.k2 : 0; a.s2 = two ? g.s2 : 0.0;
+  b.X1 = g.B1; b.ld1 = g.ldb1; b.op1 = opb1; b.K1 = g.k1;
+  b.X2 = two ? g.B2 : nullptr; b.ld2 = g.ldb2; b.op2 = opb2; b.K2 = two ? g.k2 : 0; b.s2 = 1.0;
+  const int64_t Kp = rup(2 * ((int64_t)g.k1 + (two ? g.k2 : 0)), OZ_TK);
+  const int64_t mp = rup(m, OZ_TM), np = rup(n, OZ_TN);
+  std::vector<int> lev;
+  const int nsc = oz_nsc((int)Kp, nsl, &lev);
+  size_t need = sizeof(__nv_bfloat16) * ((size_t)OZ_SMAX * mp * Kp + 2 * (size_t)OZ_SMAX * np * Kp) +
+                sizeof(int) * ((size_t)nsc * 2 * mp * np + mp + np + 64) + 8 * 256;
+  if (need > ws_bytes) { set_error_message("zgemm_ozaki: workspace too small"); return ZQ_ERR_LIMIT; }
+  if (nsc > 64) { set_error_message("zgemm_ozaki: K too large"); return ZQ_ERR_LIMIT; }
+  if (opt.structured != 0 && m != n) { set_error_message("zgemm_ozaki: structured output must be square"); return ZQ_ERR_ARG; }
+  char* p = reinterpret_cast<char*>(ws);
+  auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~(size_t)255; return q; };
+  // fixed carve-up (sized for the largest shapes) so the A slices of one call can be reused by the next
+  const int64_t cap = (int64_t)(ws_bytes / 8);
+  (void)cap;
+  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * mp * Kp));
+  __nv_bfloat16* Brs = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * np * Kp));
+  __nv_bfloat16* Bis = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * np * Kp));
+  int* parts = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nsc * 2 * mp * np));
+  int* ea = reinterpret_cast<int*>(take(sizeof(int) * mp));
+  int* eb = reinterpret_cast<int*>(take(sizeof(int) * np));
+  int* dlev = reinterpret_cast<int*>(take(sizeof(int) * 64));
+  ZQ_CUDA(cudaMemcpyAsync(dlev, lev.data(), sizeof(int) * nsc, cudaMemcpyHostToDevice, st));
+  auto grid = [](int64_t total) { int64_t x = (total + 255) / 256; return (int)(x > 16384 ? 16384 : x); };
+  if (!opt.reuse_a) {
+    k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
+    ZQ_LAUNCH_CHECK();
+    k_oz_slice<<<grid(mp * Kp), 256, 0, st>>>(a, true, m, (int)mp, (int)Kp, ea, nsl, As, nullptr, mp * Kp);
+    ZQ_LAUNCH_CHECK();
+  }
+  k_oz_exp<<<ceil_div(n * 32, 256), 256, 0, st>>>(b, false, n, (int)Kp, eb);
+  ZQ_LAUNCH_CHECK();
+  k_oz_slice<<<grid(np * Kp), 256, 0, st>>>(b, false, n, (int)np, (int)Kp, eb, nsl, Brs, Bis, np * Kp);
+  ZQ_LAUNCH_CHECK();
+  OzGemmArgs og{};
+  og.A = As; og.Bre = Brs; og.Bim = Bis; og.sa = mp * Kp; og.sb = np * Kp;
+  og.mp = (int)mp; og.np = (int)np; og.Kp = (int)Kp; og.out = parts; og.nsc = nsc;
+  og.nsl = nsl; og.lower = opt.structured != 0 ? 1 : 0;
+  const int smem = 2 * 3 * OZ_TM * OZ_LDS * (int)sizeof(__nv_bfloat16);
+  static bool attr = false;
+  if (!attr) {
+    ZQ_CUDA(cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr = true;
+  }
+  const int tm = (int)(mp / OZ_TM), tn = (int)(np / OZ_TN);
+  dim3 gg = og.lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)tm, (unsigned)tn);
+  prof_begin(PC_OZAKI, st);
+  k_oz_gemm<<<gg, OZ_THREADS, smem, st>>>(og);
+  prof_end(PC_OZAKI, st);
+  ZQ_LAUNCH_CHECK();
+  k_oz_combine<<<grid((int64_t)m * n), 256, 0, st>>>(parts, nsc, dlev, (int)mp, (int)np, ea, eb, m, n, g.alpha, g.beta,
+                                                      g.C, g.ldc, og.lower);
+  ZQ_LAUNCH_CHECK();
+  if (opt.structured != 0) {
+    k_oz_symfill<<<grid((int64_t)m * n), 256, 0, st>>>(g.C, g.ldc, m, opt.structured);
+    ZQ_LAUNCH_CHECK();
+  }
+  return ZQ_OK;
 }
 
 }  // namespace zq
+
+// Public utility: FP64-accurate complex product on the tensor cores.
+//   C = op(A) op(B) (m x n, K inner), op codes 0 N, 1 T, 2 C (conj-transpose), 3 R (conj)
+extern "C" int zq_zgemm_accurate(int opa, int opb, int m, int n, int k, const double* A, int lda, const double* B,
+                                 int ldb, double* C, int ldc, void* stream) {
+  using namespace zq;
+  if (m < 0 || n < 0 || k < 0 || opa < 0 || opa > 3 || opb < 0 || opb > 3) return ZQ_ERR_ARG;
+  if (m == 0 || n == 0) return ZQ_OK;
+  const int q = (m > n ? m : n) / 2 + 1 > (k + 1) / 2 + 16 ? (m > n ? m : n) / 2 + 1 : (k + 1) / 2 + 16;
+  const size_t bytes = ozaki_workspace_bytes(q);
+  void* ws = nullptr;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  ZQ_CUDA(cudaMallocAsync(&ws, bytes, st));
+  ZgemmArgs g{};
+  g.m = m; g.n = n; g.k1 = k;
+  g.A1 = reinterpret_cast<const double2*>(A); g.lda1 = lda;
+  g.B1 = reinterpret_cast<const double2*>(B); g.ldb1 = ldb;
+  g.alpha = make_double2(1.0, 0.0); g.beta = make_double2(0.0, 0.0);
+  g.C = reinterpret_cast<double2*>(C); g.ldc = ldc;
+  OzOpts opt{};
+  opt.slices = 8;
+  const int rc = zgemm_ozaki(opa, opb, OP_N, OP_N, g, ws, bytes, st, opt);
+  cudaFreeAsync(ws, st);
+  return rc;
+}

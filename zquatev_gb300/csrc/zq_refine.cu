@@ -213,14 +213,20 @@ size_t refine_workspace_bytes(int n, int nbq) {
   return b;
 }
 
-// accurate complex product: native FP64 (mode 0) or Ozaki-sliced tensor-core products (mode 1)
-int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st);
-size_t ozaki_workspace_bytes(int n);
-
+// accurate complex product: native FP64 (mode 0) or Ozaki-sliced tensor-core products (mode 1).
+// Structured outputs (G1, S1 Hermitian; G2, S2 antisymmetric) are made exactly
+// structured from their lower triangles, so that the symmetric part of E is R
+// exactly and the orthogonality of the update does not depend on eigenvalue gaps.
 static int zgemm_acc(int mode, int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ows, size_t ows_bytes,
-                     cudaStream_t st) {
-  if (mode == 1) return zgemm_ozaki(opa1, opb1, opa2, opb2, g, ows, ows_bytes, st);
-  return zgemm<double>(opa1, opb1, opa2, opb2, g, 1, st);
+                     cudaStream_t st, int slices, int structured, int reuse_a) {
+  if (mode == 1) {
+    OzOpts o{};
+    o.slices = slices; o.structured = structured; o.reuse_a = reuse_a;
+    return zgemm_ozaki(opa1, opb1, opa2, opb2, g, ows, ows_bytes, st, o);
+  }
+  if (int rc = zgemm<double>(opa1, opb1, opa2, opb2, g, 1, st)) return rc;
+  if (structured != 0) return structured_fill(g.C, g.ldc, g.m, structured, st);
+  return ZQ_OK;
 }
 
 int refined_solve(RefineArgs& ra) {
@@ -279,6 +285,7 @@ int refined_solve(RefineArgs& ra) {
   ZQ_LAUNCH_CHECK();
 
   // B. refinement
+  prof_begin(PC_REFINE, st);
   const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
   const int nparts = 1024;
   ra.iters = 0;
@@ -286,6 +293,9 @@ int refined_solve(RefineArgs& ra) {
   const int ne = 1024;
   std::vector<double> hemax(ne);
   for (int it = 0; it < ra.max_iter; ++it) {
+    // the first correction only has to reach ~1e-8 (the next step squares the
+    // error): 5 slices (35 bits); later steps use 8 (56 bits)
+    const int sl = (it == 0) ? 5 : 8;
     double2* U = X;
     double2* V = X + n;
     ZgemmArgs g{};
@@ -293,32 +303,32 @@ int refined_solve(RefineArgs& ra) {
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n2; g.A1 = X; g.lda1 = ldd; g.B1 = X; g.ldb1 = ldd;
     g.alpha = one; g.beta = zero; g.C = G1; g.ldc = n;
-    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 0)) return rc;
     // G2 = U^T V - V^T U
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n; g.k2 = n;
     g.A1 = U; g.lda1 = ldd; g.B1 = V; g.ldb1 = ldd; g.A2 = V; g.lda2 = ldd; g.B2 = U; g.ldb2 = ldd; g.s2 = -1.0;
     g.alpha = one; g.beta = zero; g.C = G2; g.ldc = n;
-    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 0)) return rc;
     // P1 = [A;B] U, P2 = [A;B] conj(V)
     g = ZgemmArgs{};
     g.m = n2; g.n = n; g.k1 = n; g.A1 = H0; g.lda1 = n2; g.B1 = U; g.ldb1 = ldd;
     g.alpha = one; g.beta = zero; g.C = P1; g.ldc = n2;
-    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 0, 0)) return rc;
     g.B1 = V; g.C = P2;
-    if (int rc = zgemm_acc(ra.mode, OP_N, OP_R, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_N, OP_R, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 0, 1)) return rc;
     k_hx_combine<<<grid_for((int64_t)nn), 256, 0, st>>>(P1, P2, n2, n, HX, n2);
     ZQ_LAUNCH_CHECK();
     // S1 = X^H HX ; S2 = U^T HX_bot - V^T HX_top
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n2; g.A1 = X; g.lda1 = ldd; g.B1 = HX; g.ldb1 = n2;
     g.alpha = one; g.beta = zero; g.C = S1; g.ldc = n;
-    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 0)) return rc;
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n; g.k2 = n;
     g.A1 = U; g.lda1 = ldd; g.B1 = HX + n; g.ldb1 = n2; g.A2 = V; g.lda2 = ldd; g.B2 = HX; g.ldb2 = n2; g.s2 = -1.0;
     g.alpha = one; g.beta = zero; g.C = S2; g.ldc = n;
-    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 0)) return rc;
     // lambda, delta, E
     k_oa_lambda<<<ceil_div(n, 256), 256, 0, st>>>(S1, G1, n, n, lam);
     ZQ_LAUNCH_CHECK();
@@ -345,8 +355,9 @@ int refined_solve(RefineArgs& ra) {
     k_add_c64_to_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(XEf, n2, X, ldd, n2, n);
     ZQ_LAUNCH_CHECK();
     ra.iters = it + 1;
-    if (em <= ra.tol) break;
+    if (em <= ra.tol && (ra.mode == 0 || sl == 8)) break;
   }
+  prof_end(PC_REFINE, st);
   // ascending order
   k_rank<<<ceil_div(n, 128), 128, 0, st>>>(lam, n, rank);
   ZQ_LAUNCH_CHECK();
