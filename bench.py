@@ -2,18 +2,22 @@
 
 Workload (default): one n2 = 8192 (n = 4096) random quaternion-Hermitian
 matrix, complex128, A = (X + X^H)/2, B = (Y - Y^T)/2, Re/Im ~ N(0,1), full
-eigenvectors -- the "plain FP64 GPU drop-in at scale" case. A step is one full
-solve of that matrix. Inputs (512 MiB left half) are larger than L2, so no
-extra L2 flush is needed between steps.
+eigenvectors. A step is one full solve of that matrix through the drop-in's
+default path: an FP32 decomposition refined to FP64 accuracy (Ogita-Aishima,
+products on the bf16 tensor cores by Ozaki slicing), with the plain FP64 path
+as fallback. The plain FP64 GPU path is timed on the same input beside it
+(fp64_path_ms). Inputs (512 MiB left half) are larger than L2, so no extra L2
+flush is needed between steps.
 
   value   device-resident: the input is restored from an HBM master copy
           (device-to-device) and solved through the device C ABI; ms per solve.
   e2e     the reference-facing host call (zquatev_c on a host array): H2D of
           the left half, solve, D2H of all of D and eig, per solve.
-  roofline  the dominant kernel class, timed with CUDA events on its launch
-          stream during the timed region, against the FP64 DFMA peak measured
-          here by a calibration kernel (the FP64 path does not use tensor
-          cores: DMMA issues slower than DFMA on this part).
+  roofline  the dominant kernel (the Ozaki tensor-core product), timed with
+          CUDA events on its launch stream during the timed region, executed
+          bf16 flops against MEASURED_PEAKS.json's sustained bf16 figure; the
+          FP64 path's kernels are reported against the FP64 DFMA peak measured
+          here by a calibration kernel (DMMA issues slower than DFMA).
   cpu_baseline  the oracle (numpy/scipy restatement of the reference, the only
           CPU implementation that exists on the GPU host) on a bounded n2=1024
           sample, scaled by n^3 to n2 = 8192.
@@ -228,21 +232,13 @@ def run_reference(args, rank, world):
 
 
 # --------------------------------------------------------------- GPU arm
-def profile_case(n2: int, reps: int) -> None:
-    """Plain solves of one random matrix (the command ncu captures are taken on)."""
-    from zquatev_gb300 import _lib, build, inputs, solver
-
-    if not build.up_to_date():
-        build.build()
-    n = n2 // 2
-    d = inputs.random_matrix(n, 3)
-    for _ in range(reps):
-        out = d.copy(order="F")
-        eig = np.zeros(n2)
-        rc = solver.zquatev(n2, out, n2, eig)
-        if rc != 0:
-            raise SystemExit(f"zquatev_c rc={rc}: {_lib.last_error()}")
-    print(f"profile case n2={n2} x{reps}: ok")
+def measured_peaks() -> dict:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
 
 
 def main():
@@ -254,6 +250,8 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
+
+    import ctypes
 
     import torch
 
@@ -278,11 +276,11 @@ def main():
     deig = torch.zeros(n2, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
+    def step(fn="zquatev_device"):
         work[:n].copy_(master[:n])  # restore the left half (columns 0..n-1 of D)
-        rc = solver.zquatev_device(work, deig, stream)
+        rc = getattr(lib, fn)(n2, work.data_ptr(), n2, deig.data_ptr(), stream.cuda_stream)
         if rc != 0:
-            raise RuntimeError(f"zquatev_device rc={rc}: {_lib.last_error()}")
+            raise RuntimeError(f"{fn} rc={rc}: {_lib.last_error()}")
 
     for _ in range(args.warmup):
         step()
@@ -292,9 +290,10 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
-    # timed region: K steps, events on the launching stream; kernel classes profiled
+    # timed region: K steps of the drop-in's default path (refined, FP64 fallback)
+    all_classes = sum(1 << c for c in (0, 1, 3, 4, 5, 6, 7, 9, 10))
     lib.zq_profile_reset()
-    lib.zq_profile_enable((1 << 1) | (1 << 0) | (1 << 3) | (1 << 4) | (1 << 5) | (1 << 6) | (1 << 7))
+    lib.zq_profile_enable(all_classes)
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
@@ -313,17 +312,34 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_total = float(t.item())
     ms_step = ms_total / args.steps
-    prof = {k: _lib.profile_read(k) for k in ("hemv", "trail", "formq_gemm", "apply_z", "stedc", "tridiag", "formq")}
+    prof = {k: _lib.profile_read(k) for k in ("ozaki", "refine", "tridiag", "stedc", "formq", "apply_z")}
+    oz_flops = _lib.profile_flops("ozaki") / args.steps
+    iters, last_corr, fell_back = solver.refine_stats()
 
     # accuracy of the last device solve (GPU residual; FP64 torch matmul as checker)
     acc = {}
     if not args.no_check:
-        out = work
-        eig = deig[:n]
         h = torch.from_numpy(inputs.full_from_blocks(d_host[:n, :n], d_host[n:, :n])).to(dev)
-        v = out.T  # column-major view
-        acc = {"residual": metrics.torch_residual(h, v, eig), "orthonormality": metrics.torch_orthonormality(v)}
-        del h
+        v = work.T  # column-major view
+        acc = {"residual": metrics.torch_residual(h, v, deig[:n]), "orthonormality": metrics.torch_orthonormality(v),
+               "refine_iterations": iters, "last_correction": last_corr, "fp64_fallback": fell_back}
+        w = torch.linalg.eigvalsh(h)[::2]
+        acc["eig_error"] = float((deig[:n] - w).abs().max() / w.abs().max())
+        del h, w
+
+    # the plain FP64 GPU path on the same input (the comparison the target names)
+    torch.cuda.synchronize()
+    lib.zq_profile_reset()
+    lib.zq_profile_enable(all_classes)
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    step("zquatev_fp64_device")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    lib.zq_profile_enable(0)
+    fp64_ms = f0.elapsed_time(f1)
+    fprof = {k: _lib.profile_read(k) for k in ("hemv", "trail", "formq_gemm", "apply_z", "stedc", "tridiag", "formq")}
 
     # end to end through the host C ABI (H2D + solve + D2H inside)
     e2e_ms = []
@@ -338,19 +354,21 @@ def main():
         e2e_ms.append((t1 - t0) * 1e3)
     e2e = float(np.mean(e2e_ms))
 
-    # roofline: dominant kernel class by event time
-    F = {  # executed FP64 flops per solve for each class (4M complex multiply-add = 8 flops, 3M = 6)
-        "trail": (16.0 / 3.0) * n ** 3 * 2,              # 32 n^3/3 DFMA-equivalent flops (4M, lower triangles)
-        "hemv": (16.0 / 3.0) * n ** 3 * 2,               # 4 complex matvecs per column on the lower triangles
-        "formq_gemm": 8.0 * n ** 3 * 2,                  # (8/3) n^3 CMAC in 3M = 8 n^3 DFMA
-        "apply_z": 8.0 * n ** 3,                         # (4n x n) x (n x n) real
-    }
-    per_step = {k: prof[k][0] / args.steps for k in prof}
-    dom = max(("trail", "hemv", "formq_gemm", "apply_z"), key=lambda k: per_step[k])
-    dom_ms = per_step[dom]
-    launches = prof[dom][1] / max(args.steps, 1)
-    achieved = F[dom] / (dom_ms * 1e-3) / 1e12 if dom_ms > 0 else None
-    peak = fp64_peak_tflops()
+    peaks = measured_peaks()
+    bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
+    peak_src = "MEASURED_PEAKS.json bf16_tflops_sustained (kernel timed inside a long step)"
+    if not bf16_peak:
+        bf16_peak, peak_src = 1700.0, "fallback 1.7 PFLOP/s sustained (MEASURED_PEAKS.json absent)"
+    oz_ms = prof["ozaki"][0] / args.steps
+    oz_launches = prof["ozaki"][1] / args.steps
+    achieved = oz_flops / (oz_ms * 1e-3) / 1e12 if oz_ms > 0 else None
+    fp64_peak = fp64_peak_tflops()
+    # FP64-path kernel classes against the FP64 (DFMA) pipe, executed flops per solve
+    F = {"trail": (32.0 / 3.0) * n ** 3, "hemv": (32.0 / 3.0) * n ** 3, "formq_gemm": 16.0 * n ** 3,
+         "apply_z": 8.0 * n ** 3}
+    fp64_roof = {k: {"ms": round(fprof[k][0], 2), "tflops": round(F[k] / (fprof[k][0] * 1e-3) / 1e12, 3),
+                     "frac": round(F[k] / (fprof[k][0] * 1e-3) / 1e12 / fp64_peak, 3)}
+                 for k in F if fprof[k][0] > 0}
 
     if rank == 0:
         cpu_ms, cpu_raw = cpu_sample(args.cpu_sample_n2, n2, os.cpu_count() or 1)
@@ -366,28 +384,31 @@ def main():
             "higher_is_better": False,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": "f64 (FP32 decomposition + bf16-Ozaki-refined to FP64 accuracy)",
             "data": "synthetic",
             "config": {"workload": f"single quaternion-Hermitian solve n2={n2} (n={n}), random A=(X+X^H)/2, "
-                                   "B=(Y-Y^T)/2, complex128, all eigenvectors, plain FP64 path",
+                                   "B=(Y-Y^T)/2, complex128, all eigenvectors, drop-in default path (refined)",
                        "n2": n2, "nb": int(lib.zq_get_block_size()), "parallelism": f"replicas{world}",
                        "l2": "inputs (512 MiB left half) larger than L2; restored D2D each step"},
+            "fp64_path_ms": fp64_ms,
+            "speedup_vs_fp64_path": fp64_ms / ms_step if ms_step > 0 else None,
             "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": n2 * n * 16,
                     "d2h_bytes_per_step": n2 * n2 * 16 + n * 8},
             "gpu_launches": None,
-            "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (achieved / peak) if achieved and peak else None, "traffic": None,
-                         "peak_source": "measured in this run: DFMA calibration kernel (no FP64 peak in MEASURED_PEAKS.json)",
-                         "launches_per_step": launches, "ms_per_step": dom_ms},
-            "stage_ms": {k: round(v, 3) for k, v in per_step.items()},
+            "roofline": {"bound": "tensor", "kernel": "k_oz_gemm (bf16 mma.sync, Ozaki slices)",
+                         "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": (achieved / bf16_peak) if achieved else None, "traffic": None,
+                         "peak_source": peak_src, "launches_per_step": oz_launches, "ms_per_step": oz_ms},
+            "stage_ms": {"refine": round(prof["refine"][0] / args.steps, 2), "ozaki": round(oz_ms, 2),
+                         "fp32_decomposition": round(ms_step - prof["refine"][0] / args.steps, 2)},
+            "fp64_path_roofline": {"pipe": "fp64 DFMA", "peak_tflops_measured": round(fp64_peak, 3),
+                                   "kernels": fp64_roof},
             "accuracy": acc,
             "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": os.cpu_count() or 1, "kind": "port",
                              "sample": f"one n2={args.cpu_sample_n2} solve through oracle/port.py (numpy + scipy "
                                        f"OpenBLAS/LAPACK) = {cpu_raw:.2f} s, scaled x{(n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
             "clocks": clocks,
         }
-        # kernel launches per step: counted by the profiler brackets are classes only; report the
-        # library's own launch count for one solve of this size
         line["gpu_launches"] = launches_per_solve(n) * args.steps
         print(json.dumps(line), flush=True)
     if world > 1:

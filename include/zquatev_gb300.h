@@ -66,8 +66,19 @@ int zquatev_batched_device(int count, const int* n2s, const int* ld2s, const lon
  * Ozaki-sliced bf16 tensor-core products accumulated exactly. The reference
  * has only the FP64 path (zquatev.cc:42-100). */
 int zquatev_refined_device(int n2, double* dD, int ld2, double* deig, void* stream, int mode);
-/* Iterations and final max |E| of the last refined solve on this device. */
-int zq_refine_stats(int* iters, double* last_correction);
+/* Iterations, final max |E| and whether the plain FP64 path had to be used
+ * (refinement not converged, e.g. tightly clustered eigenvalues) for the last
+ * refined solve on this device. */
+int zq_refine_stats(int* iters, double* last_correction, int* fell_back);
+
+/* Explicit paths of the host drop-in: plain FP64, or refined (with the FP64
+ * fallback). zquatev_c / ts::zquatev / zquatev_device follow the path policy
+ * set by zq_set_path: 0 FP64, 1 refined, 2 auto (default: refined for
+ * n2 >= 512, FP64 below); environment ZQ_PATH=fp64|refined|auto overrides. */
+int zquatev_fp64_c(int n2, double* D, int ld2, double* eig);
+int zquatev_refined_c(int n2, double* D, int ld2, double* eig);
+int zquatev_fp64_device(int n2, double* dD, int ld2, double* deig, void* stream);
+int zq_set_path(int path);
 
 /* FP64-accurate complex product C = op(A) op(B) (m x n, inner k; op 0 = N,
  * 1 = T, 2 = conjugate transpose, 3 = conjugate) on the bf16 tensor cores with
@@ -103,6 +114,8 @@ int zq_get_block_size(void);
 int zq_profile_enable(int mask);
 int zq_profile_read(int cls, double* total_ms, long long* launches);
 int zq_profile_reset(void);
+/* Executed arithmetic counted for a class (currently the Ozaki tensor-core product, class 9). */
+int zq_profile_flops(int cls, double* flops);
 
 /* Frees the cached device workspace of the current device. */
 int zq_release_workspace(void);

@@ -23,12 +23,13 @@ TOL = 1e-12
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
 
 
-def run(d, n2=None, ld2=None, sentinel=7.25):
+def run(d, n2=None, ld2=None, sentinel=7.25, fn=None):
+    """Plain FP64 path by default (the refined path has its own tests)."""
     out = np.array(d, dtype=np.complex128, order="F", copy=True)
     n2 = out.shape[1] if n2 is None else n2
     ld2 = out.shape[0] if ld2 is None else ld2
     eig = np.full(max(n2, 1), sentinel)
-    rc = solver.zquatev(n2, out, ld2, eig)
+    rc = (fn or solver.zquatev_fp64)(n2, out, ld2, eig)
     assert rc == 0, (rc, _lib.last_error())
     return out, eig
 
@@ -198,6 +199,24 @@ def test_larger_random(gpu):
     d = inputs.random_matrix(n, 4242)
     out, eig = run(d)
     check_solution(d, out, eig, n)
+
+
+@pytest.mark.parametrize("n", [40, 256, 700])
+def test_default_policy_drop_in(gpu, n):
+    """The drop-in call (zquatev_c, the path ts::zquatev takes) meets the same bar
+    whichever path its policy picks (FP64 below n2 = 512, refined above)."""
+    d = inputs.random_matrix(n, 8800 + n)
+    out, eig = run(d, fn=solver.zquatev)
+    check_solution(d, out, eig, n)
+
+
+def test_refined_falls_back_on_clusters(gpu):
+    """Eigenvalue clusters with 1e-6 gaps: the refined path must still return an
+    FP64-accurate result (refined or through its FP64 fallback)."""
+    n = 160
+    d, lam = inputs.clustered_matrix(n, 31)
+    out, eig = run(d, fn=solver.zquatev_refined)
+    check_solution(d, out, eig, n, ref_eig=np.sort(lam))
 
 
 def _batch(sizes, seed0):

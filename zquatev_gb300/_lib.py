@@ -23,11 +23,16 @@ SIGNATURES = {
     "zquatev_batched_device": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "zquatev_device_noalloc": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
     "zquatev_refined_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp, _c_int]),
-    "zq_refine_stats": (_c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    "zq_refine_stats": (_c_int, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)]),
+    "zquatev_fp64_c": (_c_int, [_c_int, _vp, _c_int, _vp]),
+    "zquatev_refined_c": (_c_int, [_c_int, _vp, _c_int, _vp]),
+    "zquatev_fp64_device": (_c_int, [_c_int, _vp, _c_int, _vp, _vp]),
+    "zq_set_path": (_c_int, [_c_int]),
     "zq_zgemm_accurate": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _c_int, _vp, _c_int, _vp]),
     "zq_profile_enable": (_c_int, [_c_int]),
     "zq_profile_read": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "zq_profile_reset": (_c_int, []),
+    "zq_profile_flops": (_c_int, [_c_int, ctypes.POINTER(ctypes.c_double)]),
     "zq_set_block_size": (_c_int, [_c_int]),
     "zq_get_block_size": (_c_int, []),
     "zq_release_workspace": (_c_int, []),
@@ -74,6 +79,12 @@ def check(rc: int, what: str) -> int:
 
 PROFILE_CLASSES = {"hemv": 0, "trail": 1, "panel": 2, "formq_gemm": 3, "apply_z": 4, "stedc": 5,
                    "tridiag": 6, "formq": 7, "batched": 8, "ozaki": 9, "refine": 10}
+
+
+def profile_flops(name: str) -> float:
+    f = ctypes.c_double()
+    check(load().zq_profile_flops(PROFILE_CLASSES[name], ctypes.byref(f)), "zq_profile_flops")
+    return f.value
 
 
 def profile_read(name: str) -> tuple[float, int]:

@@ -73,6 +73,13 @@ struct Prof {
 };
 static Prof g_prof;
 
+static double g_prof_flops[PC_COUNT];
+void prof_add_flops(int cls, double flops) {
+  if (!(g_prof.mask & (1 << cls))) return;
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  g_prof_flops[cls] += flops;
+}
+
 void prof_begin(int cls, cudaStream_t st) {
   if (!(g_prof.mask & (1 << cls))) return;
   std::lock_guard<std::mutex> lk(g_prof.mu);
@@ -272,8 +279,11 @@ static int check_args(int n2, const void* D, int ld2, const void* eig) {
   return ZQ_OK;
 }
 
-// host-memory drop-in
-static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors) {
+static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cudaStream_t st, int mode);
+static int path_for(int n);
+
+// host-memory drop-in (path: -1 policy, 0 FP64, 1 refined)
+static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors, int path = -1) {
   if (int rc = check_args(n2, D, ld2, eig)) return rc;
   if (n2 == 0) return ZQ_OK;
   const int n = n2 / 2;
@@ -291,7 +301,8 @@ static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors) 
     // H1: only the left half is read
     if (cudaMemcpy2DAsync(dD, sizeof(double2) * n2, D, sizeof(double2) * (size_t)ld2, sizeof(double2) * n2, n,
                           cudaMemcpyHostToDevice, c->st) != cudaSuccess) { rc = ZQ_ERR_CUDA; set_msg("H2D copy failed"); break; }
-    rc = solve_device(c, dD, n2, n, deig, vectors, c->st);
+    const int p = (path >= 0) ? path : path_for(n);
+    rc = (vectors && p == 1) ? refined_device(c, dD, n2, n, deig, c->st, 1) : solve_device(c, dD, n2, n, deig, vectors, c->st);
     if (rc) break;
     if (vectors) {
       if (cudaMemcpy2DAsync(D, sizeof(double2) * (size_t)ld2, dD, sizeof(double2) * n2, sizeof(double2) * n2, n2,
@@ -316,6 +327,7 @@ struct RefineBuffers {
   size_t bytes = 0;
   int last_iters = 0;
   double last_emax = 0.0;
+  int last_fallback = 0;
 };
 static RefineBuffers g_refine[64];
 size_t ozaki_workspace_bytes(int n);
@@ -357,18 +369,42 @@ static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* d
   ra.dc = &c->dc;
   ra.fdesc = reinterpret_cast<DgemmDescT<float>*>(desc1);
   ra.nb = nb_for(n); ra.nbq = g_nbq; ra.mode = mode;
-  ra.max_iter = 4;
+  ra.max_iter = 6;
   ra.tol = 1e-7;   // the update squares the error: |E| <= 1e-7 leaves ~1e-14
+  ra.cluster_tol = 1e-13;
+  ra.pair_eps = 1e-4;  // |E| <= 1e-4 from the formula: two more steps reach 1e-7
   if (const char* s = getenv("ZQ_REFINE_MAXIT")) ra.max_iter = atoi(s);
+  if (const char* s = getenv("ZQ_REFINE_EPS")) { const double v = atof(s); if (v > 0.0 && v < 0.5) ra.pair_eps = v; }
   ra.st = c->st;
   ZQ_CUDA(cudaEventRecord(c->ev_fork, st));
   ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
   if (int rc = refined_solve(ra)) return rc;
   rb.last_iters = ra.iters;
   rb.last_emax = ra.last_emax;
+  rb.last_fallback = 0;
+  if (!(ra.last_emax <= ra.tol) || ra.clusters < 0) {
+    // not converged (e.g. clustered eigenvalues): restore the input saved at
+    // the start of the refined solve and run the plain FP64 path
+    const double2* H0 = reinterpret_cast<const double2*>(ra.ws);
+    ZQ_CUDA(cudaMemcpy2DAsync(dD, sizeof(double2) * ldd, H0, sizeof(double2) * 2 * n, sizeof(double2) * 2 * n, n,
+                              cudaMemcpyDeviceToDevice, c->st));
+    rb.last_fallback = 1;
+    if (int rc = solve_device(c, dD, ldd, n, deig, true, c->st)) return rc;
+  }
   ZQ_CUDA(cudaEventRecord(c->ev_join, c->st));
   ZQ_CUDA(cudaStreamWaitEvent(st, c->ev_join, 0));
   return ZQ_OK;
+}
+
+// path policy of the drop-in entry points: 0 FP64, 1 refined, 2 auto
+static int g_path = 2;
+static int path_for(int n) {
+  int p = g_path;
+  if (const char* s = getenv("ZQ_PATH")) {
+    if (!strcmp(s, "fp64")) p = 0; else if (!strcmp(s, "refined")) p = 1; else if (!strcmp(s, "auto")) p = 2;
+  }
+  if (p == 2) p = (n >= 256) ? 1 : 0;
+  return p;
 }
 
 // ----------------------------------------------------------------------------
@@ -468,7 +504,32 @@ int zquatev_device(int n2, double* dD, int ld2, double* deig, void* stream) {
   Context* c = nullptr;
   if (int rc = get_context(&c)) return rc;
   std::lock_guard<std::mutex> lk(c->mu);
+  if (path_for(n2 / 2) == 1)
+    return refined_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, reinterpret_cast<cudaStream_t>(stream), 1);
   return solve_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, true, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zquatev_fp64_device(int n2, double* dD, int ld2, double* deig, void* stream) {
+  if (int rc = check_args(n2, dD, ld2, deig)) return rc;
+  if (n2 == 0) return ZQ_OK;
+  Context* c = nullptr;
+  if (int rc = get_context(&c)) return rc;
+  std::lock_guard<std::mutex> lk(c->mu);
+  return solve_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, true, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int zquatev_fp64_c(int n2, double* D, int ld2, double* eig) {
+  return zquatev_host(n2, reinterpret_cast<double2*>(D), ld2, eig, true, 0);
+}
+
+int zquatev_refined_c(int n2, double* D, int ld2, double* eig) {
+  return zquatev_host(n2, reinterpret_cast<double2*>(D), ld2, eig, true, 1);
+}
+
+int zq_set_path(int path) {
+  if (path < 0 || path > 2) { set_msg("path must be 0 (FP64), 1 (refined) or 2 (auto)"); return ZQ_ERR_ARG; }
+  g_path = path;
+  return ZQ_OK;
 }
 
 int zquatev_values_device(int n2, double* dD, int ld2, double* deig, void* stream) {
@@ -535,11 +596,12 @@ int zquatev_refined_device(int n2, double* dD, int ld2, double* deig, void* stre
   return refined_device(c, reinterpret_cast<double2*>(dD), ld2, n2 / 2, deig, reinterpret_cast<cudaStream_t>(stream), mode);
 }
 
-int zq_refine_stats(int* iters, double* last_correction) {
+int zq_refine_stats(int* iters, double* last_correction, int* fell_back) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ZQ_ERR_CUDA;
   if (iters) *iters = g_refine[dev].last_iters;
   if (last_correction) *last_correction = g_refine[dev].last_emax;
+  if (fell_back) *fell_back = g_refine[dev].last_fallback;
   return ZQ_OK;
 }
 
@@ -561,7 +623,14 @@ int zq_profile_read(int cls, double* total_ms, long long* launches) {
 int zq_profile_reset(void) {
   std::lock_guard<std::mutex> lk(g_prof.mu);
   g_prof.collect();
-  for (int i = 0; i < PC_COUNT; ++i) { g_prof.total_ms[i] = 0; g_prof.launches[i] = 0; }
+  for (int i = 0; i < PC_COUNT; ++i) { g_prof.total_ms[i] = 0; g_prof.launches[i] = 0; g_prof_flops[i] = 0; }
+  return ZQ_OK;
+}
+
+int zq_profile_flops(int cls, double* flops) {
+  if (cls < 0 || cls >= PC_COUNT || !flops) { set_msg("bad profile class"); return ZQ_ERR_ARG; }
+  std::lock_guard<std::mutex> lk(g_prof.mu);
+  *flops = g_prof_flops[cls];
   return ZQ_OK;
 }
 

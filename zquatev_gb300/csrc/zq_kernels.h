@@ -136,8 +136,13 @@ struct RefineArgs {
   DgemmDescT<float>* fdesc;    // one device descriptor slot
   int nb, nbq, mode, max_iter;
   double tol;
+  double cluster_tol;          // accepted in-cluster coupling (relative to max |lambda|)
+  double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap|
   cudaStream_t st;
   int iters; double last_emax;  // outputs
+  double last_cluster;         // in-cluster coupling of the last step (before rotation)
+  int clusters;                // clusters resolved (-1: one too large)
+  int cluster_max;             // largest cluster rotated
 };
 size_t refine_workspace_bytes(int n, int nbq);
 int refined_solve(RefineArgs& ra);

@@ -17,8 +17,8 @@
 //     int32 accumulator every 256 terms (exact), and each (level, super-chunk)
 //     writes its int32 result; level l = t + u collects the slice pairs (t, u)
 //     with t + u = l, l < S (the triangular truncation);
-//   * the combine kernel forms C = sigma_i tau_j sum_l 2^(-BETA (l + 2)) I_l in
-//     FP64.
+//   * at the end of each (level, super-chunk) the owning CTA adds
+//     sigma_i tau_j 2^(-BETA (l + 2)) I into the FP64 output.
 // With S = 7 the dropped terms are below 2^-49 of sigma_i tau_j per product,
 // i.e. FP64-level accuracy for the refinement's sums.
 //
@@ -168,14 +168,23 @@ struct OzGemmArgs {
   const __nv_bfloat16* Bim;
   int64_t sa, sb;            // slice strides (elements)
   int mp, np, Kp;
-  int* out;                  // [nsc][2][np][mp]
-  int nsc;
+  int m, n;                  // true output size
+  const int* ea;             // row exponents of A
+  const int* eb;             // column exponents of B
+  double2* C;                // FP64 output, column-major
+  int64_t ldc;
   int nsl;                   // slices per operand
   int lower;                 // 1: only tiles with I >= J (square structured outputs)
 };
 
+// 2^E as a double (E within the normal range), built from the exponent bits
+__device__ __forceinline__ double pow2i(int E) {
+  if (E < -1022) return 0.0;
+  return __longlong_as_double((long long)(1023 + E) << 52);
+}
+
 // One CTA per 64x64 tile; loops over all levels and super-chunks.
-__global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzGemmArgs g) {
+__global__ void __launch_bounds__(OZ_THREADS, 3) k_oz_gemm(OzGemmArgs g) {
   extern __shared__ __align__(16) unsigned char oz_smem[];
   __nv_bfloat16* sm = reinterpret_cast<__nv_bfloat16*>(oz_smem);
   // stage layout: A [64][LDS], Bre [64][LDS], Bim [64][LDS]; two stages
@@ -191,7 +200,6 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzGemmArgs g) {
     bi = I; bj = t - I * (I + 1) / 2;
   }
   const int i0 = bi * OZ_TM, j0 = bj * OZ_TN;
-  const int64_t mp = g.mp, np = g.np;
   int sc = 0;
   for (int lev = 0; lev < g.nsl; ++lev) {
     const int64_t total_k = (int64_t)(lev + 1) * g.Kp;
@@ -283,77 +291,37 @@ __global__ void __launch_bounds__(OZ_THREADS) k_oz_gemm(OzGemmArgs g) {
               }
         }
       }
-      // store this (level, super-chunk) partial: out[sc][ri][j][i]
-      int* o_re = g.out + ((int64_t)sc * 2 + 0) * np * mp;
-      int* o_im = g.out + ((int64_t)sc * 2 + 1) * np * mp;
+      // add this (level, super-chunk) exact result into the FP64 output:
+      //   C += 2^(ea_i + eb_j - BETA (lev + 2)) (ir + i ii)
 #pragma unroll
       for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-          const int r = i0 + wm * 32 + mt * 16 + (lane >> 2);
-          const int c = j0 + wn * 32 + nt * 8 + 2 * (lane & 3);
-          o_re[(int64_t)c * mp + r] = ir[mt][nt][0];
-          o_re[(int64_t)(c + 1) * mp + r] = ir[mt][nt][1];
-          o_re[(int64_t)c * mp + r + 8] = ir[mt][nt][2];
-          o_re[(int64_t)(c + 1) * mp + r + 8] = ir[mt][nt][3];
-          o_im[(int64_t)c * mp + r] = ii[mt][nt][0];
-          o_im[(int64_t)(c + 1) * mp + r] = ii[mt][nt][1];
-          o_im[(int64_t)c * mp + r + 8] = ii[mt][nt][2];
-          o_im[(int64_t)(c + 1) * mp + r + 8] = ii[mt][nt][3];
-        }
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int r = i0 + wm * 32 + mt * 16 + (lane >> 2) + ((q & 2) ? 8 : 0);
+            const int c = j0 + wn * 32 + nt * 8 + 2 * (lane & 3) + (q & 1);
+            if (r >= g.m || c >= g.n) continue;
+            const int e0 = g.ea[r], e1 = g.eb[c];
+            const double sc_ = (e0 > -1000 && e1 > -1000) ? pow2i(e0 + e1 - OZ_BETA * (lev + 2)) : 0.0;
+            double2* cp = g.C + r + (int64_t)c * g.ldc;
+            const double vr = sc_ * (double)ir[mt][nt][q], vi = sc_ * (double)ii[mt][nt][q];
+            if (sc == 0) *cp = make_double2(vr, vi);
+            else { double2 cur = *cp; cur.x += vr; cur.y += vi; *cp = cur; }
+          }
       ++sc;
     }
   }
 }
 
-// C = alpha * sigma_i tau_j sum_sc 2^(-BETA (lev_sc + 2)) (I_re + i I_im) + beta * C
-__global__ void k_oz_combine(const int* __restrict__ parts, int nsc, const int* __restrict__ sc_lev, int mp, int np,
-                             const int* __restrict__ ea, const int* __restrict__ eb, int m, int n, double2 alpha,
-                             double2 beta, double2* __restrict__ C, int64_t ldc, int lower) {
-  const int64_t total = (int64_t)m * n;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % m), j = (int)(t / m);
-    if (lower && (i >> 6) < (j >> 6)) continue;  // tile not computed
-    double re = 0.0, im = 0.0;
-    const int e0 = ea[i], e1 = eb[j];
-    if (e0 > -1000 && e1 > -1000) {
-      for (int q = 0; q < nsc; ++q) {
-        const int64_t o = (int64_t)j * mp + i;
-        const double sc = ldexp(1.0, e0 + e1 - OZ_BETA * (sc_lev[q] + 2));
-        re += sc * (double)parts[((int64_t)q * 2 + 0) * np * mp + o];
-        im += sc * (double)parts[((int64_t)q * 2 + 1) * np * mp + o];
-      }
-    }
-    double2 out = make_double2(alpha.x * re - alpha.y * im, alpha.x * im + alpha.y * re);
-    const int64_t oc = i + (int64_t)j * ldc;
-    if (beta.x != 0.0 || beta.y != 0.0) {
-      const double2 c = C[oc];
-      out.x += beta.x * c.x - beta.y * c.y;
-      out.y += beta.x * c.y + beta.y * c.x;
-    }
-    C[oc] = out;
-  }
-}
-
 static int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
-
-static int oz_nsc(int Kp, int nsl, std::vector<int>* lev) {
-  int nsc = 0;
-  for (int l = 0; l < nsl; ++l) {
-    const int64_t total = (int64_t)(l + 1) * Kp;
-    for (int64_t k = 0; k < total; k += OZ_SUPER) { if (lev) lev->push_back(l); ++nsc; }
-  }
-  return nsc;
-}
 
 // workspace for products with m, n <= 2 * nq and Kp <= 4 * nq + 64
 size_t ozaki_workspace_bytes(int nq) {
   const int64_t mp = rup(2 * (int64_t)nq, 64), np = rup(2 * (int64_t)nq, 64), Kp = rup(4 * (int64_t)nq, 64);
-  const int nsc = oz_nsc((int)Kp, OZ_SMAX, nullptr);
   size_t b = 0;
   b += sizeof(__nv_bfloat16) * (size_t)OZ_SMAX * mp * Kp;       // A slices
   b += sizeof(__nv_bfloat16) * (size_t)OZ_SMAX * np * Kp * 2;   // B slices (re / im forms)
-  b += sizeof(int) * (size_t)nsc * 2 * mp * np;              // int32 partials
   b += sizeof(int) * (size_t)(mp + np + 64);
   return b + 8 * 256;
 }
@@ -402,12 +370,13 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   b.X2 = two ? g.B2 : nullptr; b.ld2 = g.ldb2; b.op2 = opb2; b.K2 = two ? g.k2 : 0; b.s2 = 1.0;
   const int64_t Kp = rup(2 * ((int64_t)g.k1 + (two ? g.k2 : 0)), OZ_TK);
   const int64_t mp = rup(m, OZ_TM), np = rup(n, OZ_TN);
-  std::vector<int> lev;
-  const int nsc = oz_nsc((int)Kp, nsl, &lev);
   size_t need = sizeof(__nv_bfloat16) * ((size_t)OZ_SMAX * mp * Kp + 2 * (size_t)OZ_SMAX * np * Kp) +
-                sizeof(int) * ((size_t)nsc * 2 * mp * np + mp + np + 64) + 8 * 256;
+                sizeof(int) * (size_t)(mp + np + 64) + 8 * 256;
   if (need > ws_bytes) { set_error_message("zgemm_ozaki: workspace too small"); return ZQ_ERR_LIMIT; }
-  if (nsc > 64) { set_error_message("zgemm_ozaki: K too large"); return ZQ_ERR_LIMIT; }
+  if (g.alpha.x != 1.0 || g.alpha.y != 0.0 || g.beta.x != 0.0 || g.beta.y != 0.0) {
+    set_error_message("zgemm_ozaki: only C = op(A) op(B) (alpha 1, beta 0)");
+    return ZQ_ERR_ARG;
+  }
   if (opt.structured != 0 && m != n) { set_error_message("zgemm_ozaki: structured output must be square"); return ZQ_ERR_ARG; }
   char* p = reinterpret_cast<char*>(ws);
   auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~(size_t)255; return q; };
@@ -417,11 +386,8 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * mp * Kp));
   __nv_bfloat16* Brs = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * np * Kp));
   __nv_bfloat16* Bis = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * np * Kp));
-  int* parts = reinterpret_cast<int*>(take(sizeof(int) * (size_t)nsc * 2 * mp * np));
   int* ea = reinterpret_cast<int*>(take(sizeof(int) * mp));
   int* eb = reinterpret_cast<int*>(take(sizeof(int) * np));
-  int* dlev = reinterpret_cast<int*>(take(sizeof(int) * 64));
-  ZQ_CUDA(cudaMemcpyAsync(dlev, lev.data(), sizeof(int) * nsc, cudaMemcpyHostToDevice, st));
   auto grid = [](int64_t total) { int64_t x = (total + 255) / 256; return (int)(x > 16384 ? 16384 : x); };
   if (!opt.reuse_a) {
     k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
@@ -435,7 +401,8 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   ZQ_LAUNCH_CHECK();
   OzGemmArgs og{};
   og.A = As; og.Bre = Brs; og.Bim = Bis; og.sa = mp * Kp; og.sb = np * Kp;
-  og.mp = (int)mp; og.np = (int)np; og.Kp = (int)Kp; og.out = parts; og.nsc = nsc;
+  og.mp = (int)mp; og.np = (int)np; og.Kp = (int)Kp;
+  og.m = m; og.n = n; og.ea = ea; og.eb = eb; og.C = g.C; og.ldc = g.ldc;
   og.nsl = nsl; og.lower = opt.structured != 0 ? 1 : 0;
   const int smem = 2 * 3 * OZ_TM * OZ_LDS * (int)sizeof(__nv_bfloat16);
   static bool attr = false;
@@ -445,12 +412,15 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   }
   const int tm = (int)(mp / OZ_TM), tn = (int)(np / OZ_TN);
   dim3 gg = og.lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)tm, (unsigned)tn);
+  {
+    // executed tensor-core flops: slice pairs x (Re, Im) x tiles x 64 x 64 x Kp x 2
+    const double pairs = (double)nsl * (nsl + 1) / 2.0;
+    const double tiles = og.lower ? (double)tm * (tm + 1) / 2.0 : (double)tm * tn;
+    prof_add_flops(PC_OZAKI, pairs * 2.0 * tiles * OZ_TM * OZ_TN * (double)Kp * 2.0);
+  }
   prof_begin(PC_OZAKI, st);
   k_oz_gemm<<<gg, OZ_THREADS, smem, st>>>(og);
   prof_end(PC_OZAKI, st);
-  ZQ_LAUNCH_CHECK();
-  k_oz_combine<<<grid((int64_t)m * n), 256, 0, st>>>(parts, nsc, dlev, (int)mp, (int)np, ea, eb, m, n, g.alpha, g.beta,
-                                                      g.C, g.ldc, og.lower);
   ZQ_LAUNCH_CHECK();
   if (opt.structured != 0) {
     k_oz_symfill<<<grid((int64_t)m * n), 256, 0, st>>>(g.C, g.ldc, m, opt.structured);

@@ -28,6 +28,9 @@
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 namespace zq {
@@ -116,23 +119,29 @@ __global__ void k_oa_norms(const double2* __restrict__ S1, const double2* __rest
   }
 }
 
-// E_top (n x n) and E_bot (n x n), written as complex64 for the FP32 update,
-// plus per-block max |E| off the Kramers pairs (convergence measure).
+// E_top (n x n) and E_bot (n x n), written as complex64 for the FP32 update.
+// A pair (p, j) is corrected by the first-order formula only when its
+// coupling c = S_pj + lambda_j R_pj is small against its gap,
+// |c| <= eps_pair |lambda_j - lambda_p|; otherwise the pair belongs to an
+// eigenvalue cluster: E_pj = R_pj / 2 (orthogonalisation only) and the pair is
+// recorded, so the host can group the clusters and rotate inside them.
+// Outputs: per-block max |E| (convergence) and max in-cluster coupling
+// relative to max |lambda|.
 __global__ void k_oa_build_e(const double2* __restrict__ S1, const double2* __restrict__ S2,
                              const double2* __restrict__ G1, const double2* __restrict__ G2, int64_t ld, int n,
                              const double* __restrict__ lam, const double* __restrict__ part, int nparts,
-                             float2* __restrict__ Et, float2* __restrict__ Eb, int64_t lde, double* __restrict__ emax) {
+                             float2* __restrict__ Et, float2* __restrict__ Eb, int64_t lde, double* __restrict__ emax,
+                             int* __restrict__ pair_count, int2* __restrict__ pairs, int pair_cap, double eps_pair) {
   __shared__ double sh[32];
-  __shared__ double s_delta;
+  __shared__ double s_lm;
   if (threadIdx.x == 0) {
-    double ss = 0.0, rr = 0.0, lm = 0.0;
-    for (int q = 0; q < nparts; ++q) { ss = fmax(ss, part[3 * q]); rr = fmax(rr, part[3 * q + 1]); lm = fmax(lm, part[3 * q + 2]); }
-    // 2-norm estimates of the 2n x 2n perturbations from their largest entries
-    s_delta = 2.0 * sqrt(2.0 * n) * (ss + lm * rr);
+    double lm = 0.0;
+    for (int q = 0; q < nparts; ++q) lm = fmax(lm, part[3 * q + 2]);
+    s_lm = lm;
   }
   __syncthreads();
-  const double delta = s_delta;
-  double em = 0.0;
+  const double inv_lm = s_lm > 0.0 ? 1.0 / s_lm : 1.0;
+  double em = 0.0, cm = 0.0;
   const int64_t total = (int64_t)n * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % n), j = (int)(t / n);
@@ -145,18 +154,31 @@ __global__ void k_oa_build_e(const double2* __restrict__ S1, const double2* __re
     if (i == j) r1.x += 1.0;
     const double2 g2 = G2[o];
     const double2 r2 = make_double2(-g2.x, -g2.y);
+    const double2 s1 = S1[o], s2 = S2[o];
+    const double2 c1 = make_double2(s1.x + lj * r1.x, s1.y + lj * r1.y);
+    const double2 c2 = make_double2(s2.x + lj * r2.x, s2.y + lj * r2.y);
+    const double a1 = fmax(fabs(c1.x), fabs(c1.y)), a2 = fmax(fabs(c2.x), fabs(c2.y));
     double2 e1, e2;
-    if (i != j && fabs(gap) > delta) {
-      const double2 s1 = S1[o];
-      e1 = make_double2((s1.x + lj * r1.x) / gap, (s1.y + lj * r1.y) / gap);
+    bool cl = false;
+    if (i == j) {
+      e1 = make_double2(0.5 * r1.x, 0.5 * r1.y);
+    } else if (a1 <= eps_pair * fabs(gap)) {
+      e1 = make_double2(c1.x / gap, c1.y / gap);
     } else {
       e1 = make_double2(0.5 * r1.x, 0.5 * r1.y);
+      cl = true;
+      cm = fmax(cm, a1 * inv_lm);
     }
-    if (fabs(gap) > delta) {
-      const double2 s2 = S2[o];
-      e2 = make_double2((s2.x + lj * r2.x) / gap, (s2.y + lj * r2.y) / gap);
-    } else {
+    if (i == j || a2 > eps_pair * fabs(gap)) {
+      // i == j: the Kramers partner (same eigenvalue, zero coupling by structure)
       e2 = make_double2(0.5 * r2.x, 0.5 * r2.y);
+      if (i != j) { cl = true; cm = fmax(cm, a2 * inv_lm); }
+    } else {
+      e2 = make_double2(c2.x / gap, c2.y / gap);
+    }
+    if (cl && i < j) {
+      const int q = atomicAdd(pair_count, 1);
+      if (q < pair_cap) pairs[q] = make_int2(i, j);
     }
     Et[i + (int64_t)j * lde] = make_float2((float)e1.x, (float)e1.y);
     Eb[i + (int64_t)j * lde] = make_float2((float)e2.x, (float)e2.y);
@@ -164,7 +186,189 @@ __global__ void k_oa_build_e(const double2* __restrict__ S1, const double2* __re
     em = fmax(em, fmax(fabs(e2.x), fabs(e2.y)));
   }
   em = block_max(em, sh);
-  if (threadIdx.x == 0) emax[blockIdx.x] = em;
+  cm = block_max(cm, sh);
+  if (threadIdx.x == 0) { emax[blockIdx.x] = em; emax[gridDim.x + blockIdx.x] = cm; }
+}
+
+// ---------------------------------------------------------------- clusters
+// Gather the quaternion block of every cluster into the left half of a small
+// (2k x 2k) matrix for the batched solver. The block is the orthogonalised
+// Rayleigh block S + lbar (I - G) (lbar = the cluster's mean Rayleigh
+// quotient): the basis is only orthonormal to ~1e-7 after the FP32 start, and
+// lbar (I - G) is far larger than in-cluster gaps of 1e-6, so S alone would
+// rotate by the wrong angles.
+__global__ void k_cl_gather(const double2* __restrict__ S1, const double2* __restrict__ S2,
+                            const double2* __restrict__ G1, const double2* __restrict__ G2, int64_t lds,
+                            const double* __restrict__ lam, const int* __restrict__ members,
+                            const int* __restrict__ cstart, const long long* __restrict__ coff, int ncl,
+                            double2* __restrict__ blocks) {
+  __shared__ double sh[32];
+  const int c = blockIdx.x;
+  if (c >= ncl) return;
+  const int b = cstart[c], k = cstart[c + 1] - b;
+  double ls = 0.0;
+  for (int r = threadIdx.x; r < k; r += blockDim.x) ls += lam[members[b + r]];
+  const double lbar = block_sum(ls, sh) / k;
+  double2* D = blocks + coff[c];
+  const int k2 = 2 * k;
+  for (int t = threadIdx.x; t < k * k; t += blockDim.x) {
+    const int r = t % k, q = t / k;
+    const int gi = members[b + r], gj = members[b + q];
+    const int64_t o = gi + (int64_t)gj * lds;
+    const double2 s1 = S1[o], s2 = S2[o], g1 = G1[o], g2 = G2[o];
+    const double d = (r == q) ? 1.0 : 0.0;
+    D[r + (int64_t)q * k2] = make_double2(s1.x + lbar * (d - g1.x), s1.y - lbar * g1.y);
+    D[k + r + (int64_t)q * k2] = make_double2(s2.x - lbar * g2.x, s2.y - lbar * g2.y);
+  }
+}
+
+// X_C <- X_C W_U + J conj(X_C) W_V  (W = cluster eigenvectors, left half [W_U; W_V]);
+// cluster eigenvalues replace the Rayleigh quotients.
+__global__ void k_cl_rotate(double2* __restrict__ X, int64_t ldx, int n, const int* __restrict__ members,
+                            const int* __restrict__ cstart, const long long* __restrict__ coff, const long long* __restrict__ eoff,
+                            int ncl, const double2* __restrict__ blocks, const double* __restrict__ ceig,
+                            double2* __restrict__ tmp, double* __restrict__ lam) {
+  const int c = blockIdx.y;
+  if (c >= ncl) return;
+  const int b = cstart[c], k = cstart[c + 1] - b;
+  const double2* W = blocks + coff[c];
+  const int k2 = 2 * k;
+  // rows of the 2n x k result, one thread per (row, column)
+  const int64_t total = (int64_t)2 * n * k;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int row = (int)(t % (2 * n)), q = (int)(t / (2 * n));
+    double2 acc = make_double2(0.0, 0.0);
+    for (int p = 0; p < k; ++p) {
+      const int col = members[b + p];
+      const double2 xa = X[(row < n ? row : row - n) + (int64_t)col * ldx];
+      const double2 xb = X[(row < n ? row + n : row) + (int64_t)col * ldx];
+      // X_C row value and the partner J conj(X_C) row value (-conj(V) on top, conj(U) below)
+      const double2 x = row < n ? xa : xb;
+      const double2 y = row < n ? make_double2(-xb.x, xb.y) : make_double2(xa.x, -xa.y);
+      const double2 wu = W[p + (int64_t)q * k2], wv = W[k + p + (int64_t)q * k2];
+      cfma(acc, x, wu);
+      cfma(acc, y, wv);
+    }
+    tmp[row + (int64_t)(b + q) * 2 * n] = acc;
+    if (row == 0) lam[members[b + q]] = ceig[eoff[c] + q];
+  }
+}
+__global__ void k_cl_writeback(double2* __restrict__ X, int64_t ldx, int n, const int* __restrict__ members, int total_m,
+                               const double2* __restrict__ tmp) {
+  const int64_t total = (int64_t)2 * n * total_m;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int row = (int)(t % (2 * n)), q = (int)(t / (2 * n));
+    X[row + (int64_t)members[q] * ldx] = tmp[row + (int64_t)q * 2 * n];
+  }
+}
+
+// Quaternion congruence of a structured pair (M1 Hermitian, M2 antisymmetric,
+// the two halves of the Rayleigh or Gram matrix of X) by the cluster rotations
+// X_C <- X_C W_U + J conj(X_C) W_V. Columns first:
+//   M1[:, C] <- M1[:, C] W_U - conj(M2[:, C]) W_V
+//   M2[:, C] <- M2[:, C] W_U + conj(M1[:, C]) W_V
+// into tmp (n x m per matrix, m = all cluster members), blockIdx.z picks S or G.
+__global__ void k_cl_congr_cols(const double2* __restrict__ S1, const double2* __restrict__ S2,
+                                const double2* __restrict__ G1, const double2* __restrict__ G2, int64_t ld, int n,
+                                const int* __restrict__ members, const int* __restrict__ cstart,
+                                const long long* __restrict__ coff, int ncl, const double2* __restrict__ blocks, int m,
+                                double2* __restrict__ tmpS, double2* __restrict__ tmpG) {
+  const int c = blockIdx.y;
+  if (c >= ncl) return;
+  const double2* M1 = blockIdx.z ? G1 : S1;
+  const double2* M2 = blockIdx.z ? G2 : S2;
+  double2* T = blockIdx.z ? tmpG : tmpS;
+  const int b = cstart[c], k = cstart[c + 1] - b;
+  const double2* W = blocks + coff[c];
+  const int k2 = 2 * k;
+  const int64_t total = (int64_t)n * k;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n), q = (int)(t / n);
+    double2 a1 = make_double2(0.0, 0.0), a2 = make_double2(0.0, 0.0);
+    for (int p = 0; p < k; ++p) {
+      const int64_t o = i + (int64_t)members[b + p] * ld;
+      const double2 m1 = M1[o], m2 = M2[o];
+      const double2 wu = W[p + (int64_t)q * k2], wv = W[k + p + (int64_t)q * k2];
+      cfma(a1, m1, wu);
+      cfma(a1, make_double2(-m2.x, m2.y), wv);
+      cfma(a2, m2, wu);
+      cfma(a2, make_double2(m1.x, -m1.y), wv);
+    }
+    T[i + (int64_t)(b + q) * n] = a1;
+    T[i + (int64_t)(b + q) * n + (int64_t)n * m] = a2;
+  }
+}
+__global__ void k_cl_cols_writeback(double2* __restrict__ S1, double2* __restrict__ S2, double2* __restrict__ G1,
+                                    double2* __restrict__ G2, int64_t ld, int n, const int* __restrict__ members, int m,
+                                    const double2* __restrict__ tmpS, const double2* __restrict__ tmpG) {
+  double2* M1 = blockIdx.z ? G1 : S1;
+  double2* M2 = blockIdx.z ? G2 : S2;
+  const double2* T = blockIdx.z ? tmpG : tmpS;
+  const int64_t total = (int64_t)n * m;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % n), r = (int)(t / n);
+    const int64_t o = i + (int64_t)members[r] * ld;
+    M1[o] = T[t];
+    M2[o] = T[t + total];
+  }
+}
+// Rows second, on the column-transformed pair M':
+//   N1[C, j] = W_U^H M1'[C, j] + W_V^H M2'[C, j],  N2[C, j] = W_U^T M2'[C, j] - W_V^T M1'[C, j]
+// for member columns j; for the other columns the result's structure gives the
+// row from the (already final) column: N1[C_q, j] = conj(N1[j, C_q]),
+// N2[C_q, j] = -N2[j, C_q]. Into tmp (m x n per matrix).
+__global__ void k_cl_congr_rows(const double2* __restrict__ S1, const double2* __restrict__ S2,
+                                const double2* __restrict__ G1, const double2* __restrict__ G2, int64_t ld, int n,
+                                const int* __restrict__ members, const int* __restrict__ cstart,
+                                const long long* __restrict__ coff, int ncl, const double2* __restrict__ blocks,
+                                const int* __restrict__ pos, int m, double2* __restrict__ tmpS, double2* __restrict__ tmpG) {
+  const int c = blockIdx.y;
+  if (c >= ncl) return;
+  const double2* M1 = blockIdx.z ? G1 : S1;
+  const double2* M2 = blockIdx.z ? G2 : S2;
+  double2* T = blockIdx.z ? tmpG : tmpS;
+  const int b = cstart[c], k = cstart[c + 1] - b;
+  const double2* W = blocks + coff[c];
+  const int k2 = 2 * k;
+  const int64_t total = (int64_t)n * k;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(t % n), q = (int)(t / n);
+    double2 v1, v2;
+    if (pos[j] < 0) {
+      const int64_t o = j + (int64_t)members[b + q] * ld;
+      const double2 m1 = M1[o], m2 = M2[o];
+      v1 = make_double2(m1.x, -m1.y);
+      v2 = make_double2(-m2.x, -m2.y);
+    } else {
+      v1 = make_double2(0.0, 0.0);
+      v2 = make_double2(0.0, 0.0);
+      for (int p = 0; p < k; ++p) {
+        const int64_t o = members[b + p] + (int64_t)j * ld;
+        const double2 m1 = M1[o], m2 = M2[o];
+        const double2 wu = W[p + (int64_t)q * k2], wv = W[k + p + (int64_t)q * k2];
+        cfmac(v1, wu, m1);  // conj(wu) * m1
+        cfmac(v1, wv, m2);
+        cfma(v2, wu, m2);
+        cfma(v2, make_double2(-wv.x, -wv.y), m1);
+      }
+    }
+    T[(b + q) + (int64_t)j * m] = v1;
+    T[(b + q) + (int64_t)j * m + (int64_t)n * m] = v2;
+  }
+}
+__global__ void k_cl_rows_writeback(double2* __restrict__ S1, double2* __restrict__ S2, double2* __restrict__ G1,
+                                    double2* __restrict__ G2, int64_t ld, int n, const int* __restrict__ members, int m,
+                                    const double2* __restrict__ tmpS, const double2* __restrict__ tmpG) {
+  double2* M1 = blockIdx.z ? G1 : S1;
+  double2* M2 = blockIdx.z ? G2 : S2;
+  const double2* T = blockIdx.z ? tmpG : tmpS;
+  const int64_t total = (int64_t)n * m;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t % m), j = (int)(t / m);
+    const int64_t o = members[r] + (int64_t)j * ld;
+    M1[o] = T[t];
+    M2[o] = T[t + total];
+  }
 }
 
 // ascending order after refinement: rank of each eigenvalue
@@ -207,7 +411,7 @@ size_t refine_workspace_bytes(int n, int nbq) {
   b += sizeof(float) * nn;              // Zf
   b += tridiag_workspace_bytes<float>(n, 64);
   b += form_q_workspace_bytes(n, nbq);  // sized for double2, enough for float2
-  b += sizeof(double) * (16 * (size_t)n + 3 * 8192 + 8192 + 64);
+  b += sizeof(double) * (45 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64);
   b += sizeof(int) * (size_t)n;
   b += 64 * 256;
   return b;
@@ -226,6 +430,117 @@ static int zgemm_acc(int mode, int opa1, int opb1, int opa2, int opb2, const Zge
   }
   if (int rc = zgemm<double>(opa1, opb1, opa2, opb2, g, 1, st)) return rc;
   if (structured != 0) return structured_fill(g.C, g.ldc, g.m, structured, st);
+  return ZQ_OK;
+}
+
+// Eigenvalue clusters (consecutive eigenvalues closer than delta): for each,
+// the quaternion block [S1_CC; S2_CC] is diagonalised by the batched small
+// solver and the cluster's columns are rotated by its eigenvectors.
+long long batched_ws_stride();
+int batched_max_n();
+int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
+                   int ctas, int* dev_info, cudaStream_t st);
+size_t batched_task_bytes();
+void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot);
+
+// Rayleigh-Ritz inside each eigenvalue cluster, on the current basis: group the
+// coupled pairs (union-find), solve every cluster's orthogonalised quaternion
+// block with the batched kernel, rotate X_C, and carry the rotation through
+// S and G (rows and columns of the members), so that E is then built in the
+// rotated basis and the update stays consistent with the rotation.
+// tmpa / tmpb: 2 n^2 double2 each of scratch (free at this point of a step).
+static int resolve_clusters(RefineArgs& ra, double2* X, int64_t ldd, double2* S1, double2* S2, double2* G1, double2* G2,
+                            double* lam, const int2* dpairs, int npairs, double2* tmpa, double2* tmpb) {
+  const int n = ra.n;
+  cudaStream_t st = ra.st;
+  std::vector<int2> hp(npairs);
+  if (npairs > 0)
+    ZQ_CUDA(cudaMemcpyAsync(hp.data(), dpairs, sizeof(int2) * npairs, cudaMemcpyDeviceToHost, st));
+  ZQ_CUDA(cudaStreamSynchronize(st));
+  std::vector<int> parent(n);
+  for (int i = 0; i < n; ++i) parent[i] = i;
+  auto find = [&](int x) { while (parent[x] != x) { parent[x] = parent[parent[x]]; x = parent[x]; } return x; };
+  for (const int2& pr : hp) {
+    const int a = find(pr.x), b = find(pr.y);
+    if (a != b) parent[a > b ? a : b] = a < b ? a : b;
+  }
+  std::vector<std::vector<int>> groups(n);
+  for (int i = 0; i < n; ++i) groups[find(i)].push_back(i);
+  std::vector<int> members, cstart, pos(n, -1);
+  for (int i = 0; i < n; ++i) {
+    if (groups[i].size() < 2) continue;
+    cstart.push_back((int)members.size());
+    for (int m : groups[i]) { pos[m] = (int)members.size(); members.push_back(m); }
+  }
+  const int ncl = (int)cstart.size();
+  ra.clusters = ncl;
+  if (ncl == 0) return ZQ_OK;
+  cstart.push_back((int)members.size());
+  std::vector<long long> coff(ncl), eoff(ncl);
+  long long off = 0, eo = 0;
+  int kmax = 0;
+  for (int c = 0; c < ncl; ++c) {
+    const int k = cstart[c + 1] - cstart[c];
+    kmax = k > kmax ? k : kmax;
+    coff[c] = off; eoff[c] = eo;
+    off += 4LL * k * k;
+    eo += 2 * k;
+  }
+  if (kmax > batched_max_n()) { ra.clusters = -1; return ZQ_OK; }  // too large: leave to the FP64 fallback
+  ra.cluster_max = kmax > ra.cluster_max ? kmax : ra.cluster_max;
+  const int m = (int)members.size();
+  const int ctas = ncl < 304 ? ncl : 304;
+  const size_t tb = batched_task_bytes();
+  size_t need = sizeof(double2) * (size_t)off + sizeof(double) * (size_t)eo +
+                sizeof(int) * (members.size() + cstart.size() + 2 * ncl + 8 + (size_t)n) + sizeof(long long) * 2 * ncl +
+                tb * ncl + sizeof(double) * (size_t)batched_ws_stride() * ctas + 16 * 256;
+  void* mem = nullptr;
+  ZQ_CUDA(cudaMallocAsync(&mem, need, st));
+  char* p = reinterpret_cast<char*>(mem);
+  auto take = [&](size_t bytes) { char* q = p; p += (bytes + 255) & ~(size_t)255; return q; };
+  double2* blocks = reinterpret_cast<double2*>(take(sizeof(double2) * (size_t)off));
+  double* ceig = reinterpret_cast<double*>(take(sizeof(double) * (size_t)eo));
+  int* dmem = reinterpret_cast<int*>(take(sizeof(int) * members.size()));
+  int* dcs = reinterpret_cast<int*>(take(sizeof(int) * cstart.size()));
+  int* dpos = reinterpret_cast<int*>(take(sizeof(int) * (size_t)n));
+  long long* dco = reinterpret_cast<long long*>(take(sizeof(long long) * ncl));
+  long long* deo = reinterpret_cast<long long*>(take(sizeof(long long) * ncl));
+  int* dinf = reinterpret_cast<int*>(take(sizeof(int) * (ncl + 8)));
+  void* dtasks = take(tb * ncl);
+  double* bws = reinterpret_cast<double*>(take(sizeof(double) * (size_t)batched_ws_stride() * ctas));
+  std::vector<char> htasks(tb * ncl);
+  for (int c = 0; c < ncl; ++c) {
+    const int k = cstart[c + 1] - cstart[c];
+    batched_fill_task(htasks.data() + c * tb, coff[c], eoff[c], k, 2 * k, c);
+  }
+  ZQ_CUDA(cudaMemcpyAsync(dmem, members.data(), sizeof(int) * members.size(), cudaMemcpyHostToDevice, st));
+  ZQ_CUDA(cudaMemcpyAsync(dcs, cstart.data(), sizeof(int) * cstart.size(), cudaMemcpyHostToDevice, st));
+  ZQ_CUDA(cudaMemcpyAsync(dpos, pos.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st));
+  ZQ_CUDA(cudaMemcpyAsync(dco, coff.data(), sizeof(long long) * ncl, cudaMemcpyHostToDevice, st));
+  ZQ_CUDA(cudaMemcpyAsync(deo, eoff.data(), sizeof(long long) * ncl, cudaMemcpyHostToDevice, st));
+  ZQ_CUDA(cudaMemcpyAsync(dtasks, htasks.data(), tb * ncl, cudaMemcpyHostToDevice, st));
+  k_cl_gather<<<ncl, 256, 0, st>>>(S1, S2, G1, G2, n, lam, dmem, dcs, dco, ncl, blocks);
+  ZQ_LAUNCH_CHECK();
+  if (int rc = batched_launch(dtasks, ncl, dinf + ncl, blocks, ceig, bws, ctas, dinf, st)) return rc;
+  // X_C (2n x m scratch in tmpa)
+  const int gx = ceil_div(2 * n * kmax, 256) > 64 ? 64 : ceil_div(2 * n * kmax, 256);
+  k_cl_rotate<<<dim3(gx, ncl), 256, 0, st>>>(X, ldd, n, dmem, dcs, dco, deo, ncl, blocks, ceig, tmpa, lam);
+  ZQ_LAUNCH_CHECK();
+  k_cl_writeback<<<grid_for((int64_t)2 * n * m), 256, 0, st>>>(X, ldd, n, dmem, m, tmpa);
+  ZQ_LAUNCH_CHECK();
+  // S, G: columns, then rows (2 n m double2 of scratch per pair)
+  const int gc = ceil_div(n * kmax, 256) > 64 ? 64 : ceil_div(n * kmax, 256);
+  const int gw = grid_for((int64_t)n * m) > 4096 ? 4096 : grid_for((int64_t)n * m);
+  k_cl_congr_cols<<<dim3(gc, ncl, 2), 256, 0, st>>>(S1, S2, G1, G2, n, n, dmem, dcs, dco, ncl, blocks, m, tmpa, tmpb);
+  ZQ_LAUNCH_CHECK();
+  k_cl_cols_writeback<<<dim3(gw, 1, 2), 256, 0, st>>>(S1, S2, G1, G2, n, n, dmem, m, tmpa, tmpb);
+  ZQ_LAUNCH_CHECK();
+  k_cl_congr_rows<<<dim3(gc, ncl, 2), 256, 0, st>>>(S1, S2, G1, G2, n, n, dmem, dcs, dco, ncl, blocks, dpos, m, tmpa,
+                                                    tmpb);
+  ZQ_LAUNCH_CHECK();
+  k_cl_rows_writeback<<<dim3(gw, 1, 2), 256, 0, st>>>(S1, S2, G1, G2, n, n, dmem, m, tmpa, tmpb);
+  ZQ_LAUNCH_CHECK();
+  ZQ_CUDA(cudaFreeAsync(mem, st));
   return ZQ_OK;
 }
 
@@ -252,7 +567,7 @@ int refined_solve(RefineArgs& ra) {
   float* Zf = reinterpret_cast<float*>(take(sizeof(float) * nn));
   void* tri_ws = take(tridiag_workspace_bytes<float>(n, 64));
   void* fq_ws = take(form_q_workspace_bytes(n, ra.nbq));
-  double* sm = reinterpret_cast<double*>(take(sizeof(double) * (16 * (size_t)n + 3 * 8192 + 8192 + 64)));
+  double* sm = reinterpret_cast<double*>(take(sizeof(double) * (45 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64)));
   int* rank = reinterpret_cast<int*>(take(sizeof(int) * (size_t)n));
   double* d = sm; sm += n;
   double* e = sm; sm += 4 * (size_t)n;
@@ -262,7 +577,10 @@ int refined_solve(RefineArgs& ra) {
   double* lam = sm; sm += n;
   double* lam2 = sm; sm += n;
   double* part = sm; sm += 3 * 8192;
-  double* emax = sm;
+  double* emax = sm; sm += 2048;
+  int* pair_count = reinterpret_cast<int*>(sm); sm += 8;
+  int2* pairs = reinterpret_cast<int2*>(sm);
+  const int pair_cap = 32 * n;  // 13 n doubles above, 32 n int2 here
   const int64_t ldd = ra.ldd;
   double2* X = ra.dD;  // (U; V) lives in the output's left half
 
@@ -291,7 +609,8 @@ int refined_solve(RefineArgs& ra) {
   ra.iters = 0;
   ra.last_emax = 1.0;
   const int ne = 1024;
-  std::vector<double> hemax(ne);
+  std::vector<double> hemax(2 * ne);
+  const bool trace = getenv("ZQ_REFINE_TRACE") != nullptr;  // per-step history on stderr
   for (int it = 0; it < ra.max_iter; ++it) {
     // the first correction only has to reach ~1e-8 (the next step squares the
     // error): 5 slices (35 bits); later steps use 8 (56 bits)
@@ -329,18 +648,34 @@ int refined_solve(RefineArgs& ra) {
     g.A1 = U; g.lda1 = ldd; g.B1 = HX + n; g.ldb1 = n2; g.A2 = V; g.lda2 = ldd; g.B2 = HX; g.ldb2 = n2; g.s2 = -1.0;
     g.alpha = one; g.beta = zero; g.C = S2; g.ldc = n;
     if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 0)) return rc;
-    // lambda, delta, E
-    k_oa_lambda<<<ceil_div(n, 256), 256, 0, st>>>(S1, G1, n, n, lam);
-    ZQ_LAUNCH_CHECK();
-    k_oa_norms<<<nparts, 256, 0, st>>>(S1, S2, G1, G2, n, n, lam, part);
-    ZQ_LAUNCH_CHECK();
-    k_oa_build_e<<<ne, 256, 0, st>>>(S1, S2, G1, G2, n, n, lam, part, nparts, Et, Eb, n, emax);
-    ZQ_LAUNCH_CHECK();
-    ZQ_CUDA(cudaMemcpyAsync(hemax.data(), emax, sizeof(double) * ne, cudaMemcpyDeviceToHost, st));
-    ZQ_CUDA(cudaStreamSynchronize(st));
-    double em = 0.0;
-    for (double v : hemax) em = v > em ? v : em;
+    // Rayleigh quotients, coupling norms, E; pairs that fail the first-order
+    // test are grouped into clusters, rotated (Rayleigh-Ritz on the current
+    // basis, S and G carried along), and E is rebuilt in the rotated basis
+    double em = 0.0, cm = 0.0;
+    int hcount = 0, clusters = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+      k_oa_lambda<<<ceil_div(n, 256), 256, 0, st>>>(S1, G1, n, n, lam);
+      ZQ_LAUNCH_CHECK();
+      k_oa_norms<<<nparts, 256, 0, st>>>(S1, S2, G1, G2, n, n, lam, part);
+      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(cudaMemsetAsync(pair_count, 0, sizeof(int), st));
+      k_oa_build_e<<<ne, 256, 0, st>>>(S1, S2, G1, G2, n, n, lam, part, nparts, Et, Eb, n, emax, pair_count, pairs,
+                                       pair_cap, ra.pair_eps);
+      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(cudaMemcpyAsync(hemax.data(), emax, sizeof(double) * 2 * ne, cudaMemcpyDeviceToHost, st));
+      ZQ_CUDA(cudaMemcpyAsync(&hcount, pair_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+      ZQ_CUDA(cudaStreamSynchronize(st));
+      em = 0.0; cm = 0.0;
+      for (int q = 0; q < ne; ++q) { em = hemax[q] > em ? hemax[q] : em; cm = hemax[ne + q] > cm ? hemax[ne + q] : cm; }
+      if (pass == 1 || !(cm > ra.cluster_tol)) break;
+      if (hcount > pair_cap) { ra.clusters = -1; break; }
+      if (int rc = resolve_clusters(ra, X, ldd, S1, S2, G1, G2, lam, pairs, hcount, P1, P2)) return rc;
+      if (ra.clusters < 0) break;
+      clusters = ra.clusters;
+    }
+    if (ra.clusters < 0) break;
     ra.last_emax = em;
+    ra.last_cluster = cm;
     // X += X E_top + J conj(X) E_bot  (FP32 product, FP64 accumulation)
     k_c128_to_c64<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(X, ldd, Xf, n2, n2, n);
     ZQ_LAUNCH_CHECK();
@@ -355,6 +690,9 @@ int refined_solve(RefineArgs& ra) {
     k_add_c64_to_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(XEf, n2, X, ldd, n2, n);
     ZQ_LAUNCH_CHECK();
     ra.iters = it + 1;
+    if (trace)
+      fprintf(stderr, "zq refine n=%d step %d slices %d emax %.3e coupling %.3e pairs %d clusters %d\n", n, it, sl,
+              em, cm, hcount, clusters);
     if (em <= ra.tol && (ra.mode == 0 || sl == 8)) break;
   }
   prof_end(PC_REFINE, st);

@@ -111,6 +111,36 @@ def clustered_matrix(n: int, seed: int, ld2: int | None = None
     return pack_left_half(a, b, ld2), lam
 
 
+def clustered_matrix_device(n: int, seed: int):
+    """(D as a torch (n2, n2) complex128 CUDA tensor holding column-major D, lambda).
+
+    Large-n version of clustered_matrix: the quaternion-unitary Q is the
+    eigenvector matrix (exactly (U -V*; V U*)-structured) that the FP64 GPU path
+    returns for a random quaternion-Hermitian matrix, and H = Q diag(lam, lam) Q^H
+    is formed with torch FP64 products on the GPU.
+    """
+    import torch
+
+    from . import _lib
+
+    lib = _lib.load()
+    n2 = 2 * n
+    d = random_matrix(n, seed + 104729)
+    dq = torch.from_numpy(np.ascontiguousarray(d.T)).cuda()
+    de = torch.zeros(n2, dtype=torch.float64, device="cuda")
+    rc = lib.zquatev_fp64_device(n2, dq.data_ptr(), n2, de.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    if rc != 0:
+        raise RuntimeError(f"zquatev_fp64_device rc={rc}: {_lib.last_error()}")
+    q = dq.T  # (n2, n2) column-major view: columns are eigenvectors
+    lam = clustered_spectrum(n, seed)
+    lt = torch.from_numpy(np.concatenate([lam, lam])).cuda().to(torch.complex128)
+    h = (q * lt) @ q.conj().T
+    h = (h + h.conj().T) / 2
+    del dq, q
+    dmat = torch.ascontiguousarray(h.T) if hasattr(torch, "ascontiguousarray") else h.T.contiguous()
+    return dmat, lam
+
+
 def log_uniform_sizes(count: int, lo: int, hi: int, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64).clip(lo, hi)

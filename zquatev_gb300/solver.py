@@ -28,6 +28,28 @@ def zquatev(n2: int, d: np.ndarray, ld2: int, eig: np.ndarray) -> int:
     return _lib.load().zquatev_c(n2, d.ctypes.data, ld2, eig.ctypes.data)
 
 
+def zquatev_fp64(n2: int, d: np.ndarray, ld2: int, eig: np.ndarray) -> int:
+    """ts::zquatev on the plain FP64 path (no mixed precision)."""
+    _check_host(d, eig)
+    return _lib.load().zquatev_fp64_c(n2, d.ctypes.data, ld2, eig.ctypes.data)
+
+
+def zquatev_refined(n2: int, d: np.ndarray, ld2: int, eig: np.ndarray) -> int:
+    """ts::zquatev on the refined path (FP32 decomposition + Ogita-Aishima
+    refinement with Ozaki tensor-core products; FP64 fallback if it does not
+    converge)."""
+    _check_host(d, eig)
+    return _lib.load().zquatev_refined_c(n2, d.ctypes.data, ld2, eig.ctypes.data)
+
+
+def refine_stats() -> tuple[int, float, bool]:
+    import ctypes
+
+    it, em, fb = ctypes.c_int(), ctypes.c_double(), ctypes.c_int()
+    _lib.load().zq_refine_stats(ctypes.byref(it), ctypes.byref(em), ctypes.byref(fb))
+    return it.value, em.value, bool(fb.value)
+
+
 def eigvals(n2: int, d: np.ndarray, ld2: int, eig: np.ndarray) -> int:
     """Eigenvalues only (D is used as scratch)."""
     _check_host(d, eig)
