@@ -54,8 +54,14 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-check", action="store_true")
     p.add_argument("--cpu-sample-n2", type=int, default=1024)
+    p.add_argument("--serve-requests", type=int, default=128, help="requests per serving run (0 skips serving)")
+    p.add_argument("--serve-rates", default="0.5,1,2",
+                   help="Poisson arrival rates as multiples of the FP64 one-at-a-time capacity")
+    p.add_argument("--serve-lanes", type=int, default=4)
+    p.add_argument("--batch-count", type=int, default=4096, help="matrices in the batched run (0 skips it)")
+    p.add_argument("--profile-path", default="default", choices=["default", "fp64", "batched"])
     p.add_argument("--profile-n2", type=int, default=0,
-                   help="profiling case: run --reps solves of this size through the host C ABI and exit")
+                   help="profiling case: run --reps device-resident solves of this size (--profile-path) and exit")
     p.add_argument("--reps", type=int, default=1)
     return p.parse_args()
 
@@ -231,6 +237,250 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ profiling case
+def profile_case(n2: int, reps: int, path: str):
+    """Small fixed workload for ncu captures: `reps` device-resident solves of
+    one random n2 matrix (default path or plain FP64), or one batched launch of
+    `reps` x 64 matrices with n2 = n2 (--profile-path batched)."""
+    import torch
+
+    from zquatev_gb300 import _lib, build, inputs
+
+    if not build.up_to_date():
+        build.build()
+    lib = _lib.load()
+    n = n2 // 2
+    st = torch.cuda.current_stream().cuda_stream
+    if path == "batched":
+        count = 64 * reps
+        d = inputs.random_matrix(n, 11)
+        one = torch.from_numpy(np.ascontiguousarray(d.T).reshape(-1))
+        buf = one.repeat(count).cuda()
+        deig = torch.zeros(count * n, dtype=torch.float64, device="cuda")
+        n2s = np.full(count, n2, np.int32)
+        offs = (np.arange(count, dtype=np.int64) * n2 * n2)
+        eoffs = (np.arange(count, dtype=np.int64) * n)
+        rc = lib.zquatev_batched_device(count, n2s.ctypes.data, n2s.ctypes.data, offs.ctypes.data, eoffs.ctypes.data,
+                                        buf.data_ptr(), deig.data_ptr(), st)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "batched", "n2": n2, "count": count, "rc": rc}))
+        return
+    d = inputs.random_matrix(n, 11)
+    master = torch.from_numpy(np.ascontiguousarray(d.T)).cuda()
+    work = torch.empty_like(master)
+    deig = torch.zeros(n2, dtype=torch.float64, device="cuda")
+    fn = lib.zquatev_device if path == "default" else lib.zquatev_fp64_device
+    for _ in range(reps):
+        work.copy_(master)
+        rc = fn(n2, work.data_ptr(), n2, deig.data_ptr(), st)
+        if rc != 0:
+            raise RuntimeError(f"rc={rc}: {_lib.last_error()}")
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": path, "n2": n2, "reps": reps}))
+
+
+# ---------------------------------------------------------- batched solves
+def batched_case(count: int, fp64_peak: float, seed: int = 2024) -> dict:
+    """4096 independent matrices, n log-uniform in [8, 256], solved by one call
+    of the batched entry point (persistent kernel); against the plain FP64
+    drop-in looped over a 1-in-16 sample of the same matrices (scaled)."""
+    import torch
+
+    from zquatev_gb300 import _lib, inputs
+
+    lib = _lib.load()
+    st = torch.cuda.current_stream().cuda_stream
+    ns = inputs.log_uniform_sizes(count, 8, 256, seed).astype(np.int64)
+    n2s = (2 * ns).astype(np.int32)
+    sizes = (2 * ns) ** 2
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    eoffs = np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int64)
+    host = np.empty(int(sizes.sum()), np.complex128)
+    for i, n in enumerate(ns):
+        host[offs[i]:offs[i] + sizes[i]] = inputs.random_matrix(int(n), seed * 7 + i).ravel(order="F")
+    master = torch.from_numpy(host).cuda()
+    work = torch.empty_like(master)
+    deig = torch.zeros(int(ns.sum()), dtype=torch.float64, device="cuda")
+
+    def run():
+        rc = lib.zquatev_batched_device(count, n2s.ctypes.data, n2s.ctypes.data, offs.ctypes.data, eoffs.ctypes.data,
+                                        work.data_ptr(), deig.data_ptr(), st)
+        if rc != 0:
+            raise RuntimeError(f"batched rc={rc}: {_lib.last_error()}")
+
+    times = []
+    launches = 0
+    for i in range(4):
+        work.copy_(master)
+        torch.cuda.synchronize()
+        lc0 = lib.zq_launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run()
+        e1.record()
+        torch.cuda.synchronize()
+        if i >= 1:
+            times.append(e0.elapsed_time(e1))
+            launches = lib.zq_launch_count() - lc0
+    ms = float(np.median(times))
+    # accuracy on a few of the results (GPU residual)
+    from zquatev_gb300 import metrics
+
+    worst = 0.0
+    for i in list(range(0, count, max(1, count // 16)))[:16]:
+        n = int(ns[i])
+        d = host[offs[i]:offs[i] + sizes[i]].reshape(2 * n, 2 * n, order="F")
+        h = torch.from_numpy(inputs.full_from_blocks(d[:n, :n], d[n:, :n])).cuda()
+        v = work[offs[i]:offs[i] + sizes[i]].view(2 * n, 2 * n).T
+        worst = max(worst, metrics.torch_residual(h, v, deig[eoffs[i]:eoffs[i] + n]))
+    # plain FP64 drop-in, one matrix after the other, on every 16th matrix
+    work.copy_(master)
+    sample = list(range(0, count, 16))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in sample:
+        rc = lib.zquatev_fp64_device(int(n2s[i]), work.data_ptr() + 16 * int(offs[i]), int(n2s[i]),
+                                     deig.data_ptr() + 8 * int(eoffs[i]), st)
+        assert rc == 0
+    torch.cuda.synchronize()
+    loop_s = (time.perf_counter() - t0) * count / len(sample)
+    flops = float(((64.0 / 3.0 + 16.0) * ns.astype(np.float64) ** 3).sum())
+    del master, work
+    return {"workload": f"{count} matrices, n log-uniform in [8, 256] (n2 16..512), random as config 0, per-matrix seeds",
+            "ms": ms, "solves_per_s": count / (ms * 1e-3), "gpu_launches": int(launches),
+            "fp64_loop_solves_per_s": count / loop_s, "speedup_vs_fp64_loop": loop_s / (ms * 1e-3),
+            "fp64_loop_sample": f"{len(sample)} matrices (every 16th), scaled x{count / len(sample):.0f}",
+            "algorithmic_tflops": flops / (ms * 1e-3) / 1e12,
+            "fp64_frac": flops / (ms * 1e-3) / 1e12 / fp64_peak if fp64_peak else None,
+            "max_residual_sampled": worst}
+
+
+# --------------------------------------------------------------- serving
+def serving_requests(count: int, seed: int = 4242):
+    """Mixed stream: n log-uniform in [32, 2048]; 70% random (as config 0),
+    30% clustered spectra (as config 3: 20% of the values in clusters of 8
+    with gaps 1e-6)."""
+    from zquatev_gb300 import inputs
+
+    rng = np.random.default_rng(seed)
+    ns = inputs.log_uniform_sizes(count, 32, 2048, seed)
+    clustered = rng.random(count) < 0.3
+    mats = []
+    for i, (n, cl) in enumerate(zip(ns, clustered)):
+        n = int(n)
+        if cl:
+            dm, _ = inputs.clustered_matrix_device(n, seed + i)
+            mats.append(np.asfortranarray(dm.cpu().numpy().T))
+            del dm
+        else:
+            mats.append(inputs.random_matrix(n, seed + i))
+    return mats, clustered
+
+
+def _fresh(mats):
+    return [(np.array(d, order="F", copy=True), np.zeros(d.shape[1])) for d in mats]
+
+
+def serve_server(mats, arrivals, lanes: int):
+    from zquatev_gb300.serve import Server
+
+    bufs = _fresh(mats)
+    with Server(lanes=lanes) as srv:
+        ids = []
+        t0 = time.perf_counter()
+        for d, (o, e), a in zip(mats, bufs, arrivals):
+            wait = a - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            ids.append(srv.submit(d.shape[1], o, d.shape[0], e))
+        res = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    assert all(info == 0 for info, _ in res), [info for info, _ in res]
+    lat = np.array([t["done"] - t["submit"] for _, t in res])
+    span = max(t["done"] for _, t in res) - min(t["submit"] for _, t in res)
+    paths = {}
+    for _, t in res:
+        paths[t["path"]] = paths.get(t["path"], 0) + 1
+    return bufs, {"solves_per_s": len(mats) / (span * 1e-3), "p50_ms": float(np.percentile(lat, 50)),
+                  "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                  "hbm_mean_reserved_gb": st["mean_reserved_bytes"] / 1e9,
+                  "hbm_peak_reserved_gb": st["peak_reserved_bytes"] / 1e9,
+                  "batches": st["batches"], "paths": paths}
+
+
+def serve_fp64_serial(mats, arrivals):
+    """The same stream served one request at a time, in arrival order, by the
+    plain FP64 drop-in (zquatev_fp64_c on the host arrays)."""
+    from zquatev_gb300 import _lib, solver
+
+    lib = _lib.load()
+    bufs = _fresh(mats)
+    lat, done = [], []
+    busy = 0.0
+    t0 = time.perf_counter()
+    for (o, e), a in zip(bufs, arrivals):
+        now = time.perf_counter() - t0
+        if now < a:
+            time.sleep(a - now)
+        s0 = time.perf_counter()
+        rc = solver.zquatev_fp64(o.shape[1], o, o.shape[0], e)
+        t = time.perf_counter() - t0
+        assert rc == 0
+        busy_i = time.perf_counter() - s0
+        busy += busy_i * lib.zq_solve_footprint(o.shape[1], 0)
+        lat.append((t - a) * 1e3)
+        done.append(t)
+    lat = np.array(lat)
+    span = done[-1] - arrivals[0]
+    return bufs, {"solves_per_s": len(mats) / span, "p50_ms": float(np.percentile(lat, 50)),
+                  "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                  "hbm_mean_reserved_gb": busy / span / 1e9,
+                  "hbm_peak_reserved_gb": max(lib.zq_solve_footprint(d.shape[1], 0) for d, _ in bufs) / 1e9}
+
+
+def serving_case(count: int, rates: list[float], lanes: int) -> dict:
+    import torch
+
+    from zquatev_gb300 import inputs, metrics
+
+    t_gen = time.perf_counter()
+    mats, clustered = serving_requests(count)
+    t_gen = time.perf_counter() - t_gen
+    # capacity of the one-at-a-time FP64 drop-in: everything arriving at t = 0
+    zero = np.zeros(count)
+    _, fp_sat = serve_fp64_serial(mats, zero)
+    bufs, sv_sat = serve_server(mats, zero, lanes)
+    # accuracy of every served result (GPU residual, FP64 torch as the checker)
+    worst_res, worst_eig = 0.0, 0.0
+    for d, (o, e) in zip(mats, bufs):
+        n = d.shape[1] // 2
+        h = torch.from_numpy(inputs.full_from_blocks(d[:n, :n], d[n:, :n])).cuda()
+        v = torch.from_numpy(np.ascontiguousarray(o.T)).cuda().T
+        ev = torch.from_numpy(e[:n]).cuda()
+        worst_res = max(worst_res, metrics.torch_residual(h, v, ev))
+        w = torch.linalg.eigvalsh(h)[::2]
+        worst_eig = max(worst_eig, float((ev - w).abs().max() / w.abs().max()))
+        del h, v, w
+    mu = fp_sat["solves_per_s"]
+    runs = []
+    rng = np.random.default_rng(99)
+    for r in rates:
+        lam = r * mu
+        arr = np.cumsum(rng.exponential(1.0 / lam, count))
+        arr -= arr[0]
+        _, fp = serve_fp64_serial(mats, arr)
+        _, sv = serve_server(mats, arr, lanes)
+        runs.append({"rate_per_s": lam, "rate_x_fp64_capacity": r, "server": sv, "fp64_serial": fp})
+    sizes = [d.shape[1] for d in mats]
+    return {"workload": f"{count} requests, n log-uniform in [32, 2048] (n2 {min(sizes)}..{max(sizes)}), "
+                        f"{int(clustered.sum())} clustered (config 3 style) + {count - int(clustered.sum())} random, "
+                        "Poisson arrivals; host arrays in, host arrays out",
+            "lanes": lanes, "generation_s": t_gen,
+            "saturation": {"server": sv_sat, "fp64_serial": fp_sat,
+                           "speedup": sv_sat["solves_per_s"] / fp_sat["solves_per_s"]},
+            "rates": runs, "max_residual": worst_res, "max_eig_error": worst_eig}
+
+
 # --------------------------------------------------------------- GPU arm
 def measured_peaks() -> dict:
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -245,7 +495,7 @@ def main():
     args = parse()
     rank, world, local = dist_info()
     if args.profile_n2:
-        profile_case(args.profile_n2, args.reps)
+        profile_case(args.profile_n2, args.reps, args.profile_path)
         return
     if args.impl == "reference":
         run_reference(args, rank, world)
@@ -296,6 +546,7 @@ def main():
     lib.zq_profile_enable(all_classes)
     barrier()
     torch.cuda.synchronize()
+    launches0 = lib.zq_launch_count()
     with ClockSampler(local) as clk:
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -305,6 +556,7 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
     barrier()
+    launches = lib.zq_launch_count() - launches0
     lib.zq_profile_enable(0)
     ms_total = e0.elapsed_time(e1)
     if world > 1:
@@ -370,6 +622,13 @@ def main():
                      "frac": round(F[k] / (fprof[k][0] * 1e-3) / 1e12 / fp64_peak, 3)}
                  for k in F if fprof[k][0] > 0}
 
+    del master, work
+    torch.cuda.empty_cache()
+    batched = batched_case(args.batch_count, fp64_peak) if (rank == 0 and args.batch_count > 0) else None
+    serving = None
+    if rank == 0 and args.serve_requests > 0:
+        serving = serving_case(args.serve_requests, [float(x) for x in args.serve_rates.split(",")], args.serve_lanes)
+
     if rank == 0:
         cpu_ms, cpu_raw = cpu_sample(args.cpu_sample_n2, n2, os.cpu_count() or 1)
         clocks = clk.summary()
@@ -409,39 +668,20 @@ def main():
                                        f"OpenBLAS/LAPACK) = {cpu_raw:.2f} s, scaled x{(n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
             "clocks": clocks,
         }
-        line["gpu_launches"] = launches_per_solve(n) * args.steps
+        line["gpu_launches"] = int(launches)
+        if serving is not None:
+            ref_rate = min(serving["rates"], key=lambda r: abs(r["rate_x_fp64_capacity"] - 1.0))
+            line["mixed_stream"] = {
+                "solves_per_s": serving["saturation"]["server"]["solves_per_s"],
+                "fp64_serial_solves_per_s": serving["saturation"]["fp64_serial"]["solves_per_s"],
+                "p99_ms": ref_rate["server"]["p99_ms"], "fp64_serial_p99_ms": ref_rate["fp64_serial"]["p99_ms"],
+                "p99_at_rate_per_s": ref_rate["rate_per_s"], "max_residual": serving["max_residual"]}
+            line["serving"] = serving
+        if batched is not None:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-
-
-def launches_per_solve(n: int, nb: int = 32, nbq: int = 64) -> int:
-    """Kernel launches of one vectors solve (counted from the launch sequence)."""
-    cnt = 0
-    for p in range(0, n, nb):
-        nbp = min(nb, n - p)
-        for k in range(nbp):
-            j = p + k
-            L = n - 1 - j
-            cnt += 1
-            if L < 1:
-                continue
-            cnt += 1 + (1 if (L >= 2 and k > 0) else 0) + (1 if L >= 2 else 0) + 1
-        if p + nbp < n:
-            cnt += 2
-    cnt += 1  # phase
-    # D&C: per depth leaf + 6 kernels; plus scale/unscale
-    depth = 0
-    m = n
-    while m > 1:
-        m = (m + 1) // 2
-        depth += 1
-    cnt += 4 + 7 * (depth + 1)
-    # Q formation: init + per block (pack, build_t, 8 GEMMs (+ up to 8 split reduces))
-    nref = max(n - 2, 0)
-    cnt += 1 + ((nref + nbq - 1) // nbq) * (2 + 8 + 4)
-    cnt += 2  # apply_z, symfill
-    return cnt
 
 
 if __name__ == "__main__":

@@ -117,8 +117,63 @@ int zq_profile_reset(void);
 /* Executed arithmetic counted for a class (currently the Ozaki tensor-core product, class 9). */
 int zq_profile_flops(int cls, double* flops);
 
+/* Kernels this library has launched since it was loaded (all devices, all
+ * entry points; every launch is counted on the host right after it is made). */
+long long zq_launch_count(void);
+
 /* Frees the cached device workspace of the current device. */
 int zq_release_workspace(void);
+
+/* ---------------------------------------------------------------- serving
+ * A request server on the current device: ts::zquatev calls (zquatev.h:54) on
+ * host arrays, submitted from any thread and solved as they arrive.
+ * A request's footprint is its device matrix (n2 x n2 complex) plus
+ * eigenvalues plus the workspace of its solve; requests are admitted in
+ * arrival order while the admitted footprints fit hbm_budget_bytes (<= 0:
+ * 80% of the free device memory at creation). An admitted request's matrix is
+ * copied to the device at once and stays there until its result is copied
+ * back into D and eig. Requests with n2 <= 512 are solved together in
+ * launches of the persistent batched kernel (every one that is ready when a
+ * batch slot frees up, at most max_batch); larger ones run on `lanes`
+ * concurrent lanes through the drop-in's default path (refined, FP64
+ * fallback). D and eig must stay valid until zq_server_wait returns for the
+ * request. No counterpart in the reference. */
+typedef struct zq_server zq_server;
+typedef struct zq_server_stats {
+  long long submitted, completed;
+  long long batches, batched_solves;      /* batched-kernel launches and the requests they solved */
+  long long lane_solves, refined_solves, fp64_solves, fallbacks;
+  long long queued;                       /* waiting for admission */
+  long long in_flight;                    /* admitted, not finished */
+  int lanes;
+  double budget_bytes;
+  double reserved_bytes;                  /* admitted footprints now */
+  double peak_reserved_bytes;
+  double mean_reserved_bytes;             /* time average from the first submission */
+  double device_used_bytes;               /* device memory in use (all users) at the call */
+} zq_server_stats;
+
+/* Device bytes one solve of size n2 holds: its n2 x n2 matrix, eigenvalues
+ * and workspace. path: 0 FP64, 1 refined (FP64 fallback included), 2 batched
+ * kernel (n2 <= 512), -1 the one the server would pick. The server's
+ * admission charges this figure. Negative on bad arguments. */
+long long zq_solve_footprint(int n2, int path);
+
+/* NULL on failure (zq_last_error). */
+zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch);
+/* Request id (>= 0), or a negative code: argument errors as zquatev_c, -103 if
+ * the footprint can never fit the budget. */
+long long zq_server_submit(zq_server* s, int n2, double* D, int ld2, double* eig);
+/* 1 finished, 0 not yet, -5 unknown id. */
+int zq_server_test(zq_server* s, long long id);
+/* Blocks until the request finished and returns its info. times_ms (4
+ * doubles, may be NULL): submission, admission, start and end of the solve,
+ * in ms since the server was created. path (may be NULL): 0 FP64, 1 refined,
+ * 2 batched kernel, 3 refined with FP64 fallback. The id is released. */
+int zq_server_wait(zq_server* s, long long id, double* times_ms, int* path);
+int zq_server_stats_read(zq_server* s, zq_server_stats* out);
+/* Waits for every submitted request, then stops the workers and frees the server. */
+int zq_server_destroy(zq_server* s);
 
 const char* zq_last_error(void);
 int zq_version(void);

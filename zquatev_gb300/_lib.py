@@ -38,7 +38,23 @@ SIGNATURES = {
     "zq_release_workspace": (_c_int, []),
     "zq_last_error": (ctypes.c_char_p, []),
     "zq_version": (_c_int, []),
+    "zq_launch_count": (_c_ll, []),
+    "zq_solve_footprint": (_c_ll, [_c_int, _c_int]),
+    "zq_server_create": (_vp, [_c_ll, _c_int, _c_int]),
+    "zq_server_submit": (_c_ll, [_vp, _c_int, _vp, _c_int, _vp]),
+    "zq_server_test": (_c_int, [_vp, _c_ll]),
+    "zq_server_wait": (_c_int, [_vp, _c_ll, _vp, _vp]),
+    "zq_server_stats_read": (_c_int, [_vp, _vp]),
+    "zq_server_destroy": (_c_int, [_vp]),
 }
+
+
+class ServerStats(ctypes.Structure):
+    """zq_server_stats (include/zquatev_gb300.h)."""
+    _fields_ = [(name, ctypes.c_longlong) for name in (
+        "submitted", "completed", "batches", "batched_solves", "lane_solves", "refined_solves", "fp64_solves",
+        "fallbacks", "queued", "in_flight")] + [("lanes", ctypes.c_int)] + [(name, ctypes.c_double) for name in (
+            "budget_bytes", "reserved_bytes", "peak_reserved_bytes", "mean_reserved_bytes", "device_used_bytes")]
 # the reference's C++ symbol ts::zquatev(int, std::complex<double>*, int, double*)
 REFERENCE_SYMBOL = "_ZN2ts7zquatevEiPSt7complexIdEiPd"
 

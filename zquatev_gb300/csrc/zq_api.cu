@@ -19,9 +19,11 @@
 //   * eig[n..] is left untouched, as in the reference.
 #include "zq_common.cuh"
 #include "zq_kernels.h"
+#include "zq_context.h"
 #include "../../include/zquatev_gb300.h"
 
 #include <algorithm>
+#include <atomic>
 #include <complex>
 #include <cstdlib>
 #include <cstring>
@@ -32,6 +34,9 @@
 namespace zq {
 
 static thread_local std::string g_last_error;
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line) {
   char buf[512];
@@ -99,20 +104,6 @@ void prof_end(int cls, cudaStream_t st) {
   if (g_prof.pairs.size() > 16384) g_prof.collect();
 }
 
-// ----------------------------------------------------------------------------
-// per-device context: streams, events, growable workspace, cached D&C plan
-// ----------------------------------------------------------------------------
-struct Context {
-  int device = -1;
-  cudaStream_t st = nullptr, st2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  void* ws = nullptr;
-  size_t ws_bytes = 0;
-  int dc_n = -1;
-  DcPlan dc;
-  std::mutex mu;
-};
-
 static std::mutex g_ctx_mu;
 static Context* g_ctx[64];
 static int g_nb = 32;   // panel width (autotuned table may override per n)
@@ -124,18 +115,53 @@ static int nb_for(int n) {
   return g_nb;
 }
 
+int context_create(int device, Context** out) {
+  Context* c = new Context();
+  c->device = device;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    set_last_error(e, "context streams/events", __FILE__, __LINE__);
+    context_destroy(c);
+    return ZQ_ERR_CUDA;
+  }
+  *out = c;
+  return ZQ_OK;
+}
+
+void context_destroy(Context* c) {
+  if (!c) return;
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->st2) cudaStreamSynchronize(c->st2);
+  if (c->ws && !c->ws_external) cudaFree(c->ws);
+  if (c->rb.dev && !c->rb.external) cudaFree(c->rb.dev);
+  if (c->bb.dev) cudaFree(c->bb.dev);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->st) cudaStreamDestroy(c->st);
+  if (c->st2) cudaStreamDestroy(c->st2);
+  delete c;
+}
+
+void context_bind(Context* c, void* ws, size_t ws_bytes, void* rws, size_t rws_bytes) {
+  if (c->ws && !c->ws_external) cudaFree(c->ws);
+  if (c->rb.dev && !c->rb.external) cudaFree(c->rb.dev);
+  c->ws = ws; c->ws_bytes = ws ? ws_bytes : 0; c->ws_external = ws != nullptr;
+  c->rb.dev = rws; c->rb.bytes = rws ? rws_bytes : 0; c->rb.external = rws != nullptr;
+  c->dc_n = -1;  // the D&C plan lives in the workspace: upload again
+}
+
 static int get_context(Context** out) {
   int dev = 0;
   ZQ_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) { set_msg("device ordinal out of range"); return ZQ_ERR_ARG; }
   std::lock_guard<std::mutex> lk(g_ctx_mu);
   if (!g_ctx[dev]) {
-    Context* c = new Context();
-    c->device = dev;
-    ZQ_CUDA(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
-    ZQ_CUDA(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
-    ZQ_CUDA(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-    ZQ_CUDA(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+    Context* c = nullptr;
+    if (int rc = context_create(dev, &c)) return rc;
     g_ctx[dev] = c;
   }
   *out = g_ctx[dev];
@@ -160,8 +186,17 @@ static Layout layout_for(int n, int nbmax, int nbq, size_t nnodes, size_t ndescs
   return L;
 }
 
-static int ensure_ws(Context* c, size_t bytes) {
+void solve_workspace_bytes(int n, size_t* fp64_bytes, size_t* refine_bytes) {
+  DcPlan probe;
+  probe.build(n);
+  const Layout L = layout_for(n, 64, g_nbq, probe.num_nodes(), probe.num_descs());
+  if (fp64_bytes) *fp64_bytes = L.total;
+  if (refine_bytes) *refine_bytes = refine_workspace_bytes(n, g_nbq) + ozaki_workspace_bytes(n) + 4096 + 256;
+}
+
+int ensure_ws(Context* c, size_t bytes) {
   if (c->ws_bytes >= bytes) return ZQ_OK;
+  if (c->ws_external) { set_msg("bound workspace too small"); return ZQ_ERR_ARG; }
   if (c->ws) { cudaStreamSynchronize(c->st); cudaStreamSynchronize(c->st2); cudaFree(c->ws); c->ws = nullptr; c->ws_bytes = 0; }
   ZQ_CUDA(cudaMalloc(&c->ws, bytes));
   c->ws_bytes = bytes;
@@ -196,7 +231,7 @@ struct StageTimer {
   }
 };
 
-static int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool vectors, cudaStream_t st) {
+int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool vectors, cudaStream_t st) {
   const int nb = nb_for(n);
   const char* tenv = getenv("ZQ_TIMING");
   StageTimer tm(tenv && tenv[0] == '1');
@@ -279,8 +314,6 @@ static int check_args(int n2, const void* D, int ld2, const void* eig) {
   return ZQ_OK;
 }
 
-static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cudaStream_t st, int mode);
-static int path_for(int n);
 
 // host-memory drop-in (path: -1 policy, 0 FP64, 1 refined)
 static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors, int path = -1) {
@@ -322,17 +355,8 @@ static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors, 
 // ----------------------------------------------------------------------------
 // refined (mixed-precision) path
 // ----------------------------------------------------------------------------
-struct RefineBuffers {
-  void* dev = nullptr;
-  size_t bytes = 0;
-  int last_iters = 0;
-  double last_emax = 0.0;
-  int last_fallback = 0;
-};
-static RefineBuffers g_refine[64];
-size_t ozaki_workspace_bytes(int n);
 
-static int ensure_plan(Context* c, int n) {
+int ensure_plan(Context* c, int n) {
   if (c->dc_n == n) return ZQ_OK;
   DcPlan probe;
   probe.build(n);
@@ -348,11 +372,12 @@ static int ensure_plan(Context* c, int n) {
   return ZQ_OK;
 }
 
-static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cudaStream_t st, int mode) {
+int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cudaStream_t st, int mode) {
   if (int rc = ensure_plan(c, n)) return rc;
-  RefineBuffers& rb = g_refine[c->device];
+  RefineBuffers& rb = c->rb;
   const size_t need = refine_workspace_bytes(n, g_nbq) + (mode == 1 ? ozaki_workspace_bytes(n) : 0) + 4096;
   if (rb.bytes < need) {
+    if (rb.external) { set_msg("bound refinement workspace too small"); return ZQ_ERR_ARG; }
     if (rb.dev) { cudaStreamSynchronize(c->st); cudaFree(rb.dev); rb.dev = nullptr; rb.bytes = 0; }
     ZQ_CUDA(cudaMalloc(&rb.dev, need));
     rb.bytes = need;
@@ -398,7 +423,7 @@ static int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* d
 
 // path policy of the drop-in entry points: 0 FP64, 1 refined, 2 auto
 static int g_path = 2;
-static int path_for(int n) {
+int path_for(int n) {
   int p = g_path;
   if (const char* s = getenv("ZQ_PATH")) {
     if (!strcmp(s, "fp64")) p = 0; else if (!strcmp(s, "refined")) p = 1; else if (!strcmp(s, "auto")) p = 2;
@@ -411,19 +436,7 @@ static int path_for(int n) {
 // batched: small matrices (n <= batched_max_n()) in one persistent kernel,
 // larger ones through the per-matrix path on the same stream
 // ----------------------------------------------------------------------------
-long long batched_ws_stride();
-int batched_max_n();
-int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
-                   int ctas, int* dev_info, cudaStream_t st);
-size_t batched_task_bytes();
-void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot);
 
-struct BatchBuffers {
-  void* dev = nullptr;
-  size_t bytes = 0;
-  std::vector<char> host_tasks;
-};
-static BatchBuffers g_batch[64];
 static int g_batch_ctas_per_sm = 2;
 
 static int batched_solve(int count, const int* n2s, const int* ld2s, const long long* offs, const long long* eoffs,
@@ -452,7 +465,7 @@ static int batched_solve(int count, const int* n2s, const int* ld2s, const long 
     const size_t info_bytes = align256(sizeof(int) * small.size() + sizeof(int));
     const size_t ws_bytes = sizeof(double) * (size_t)batched_ws_stride() * ctas;
     const size_t need = task_bytes + info_bytes + ws_bytes;
-    BatchBuffers& bb = g_batch[c->device];
+    BatchBuffers& bb = c->bb;
     if (bb.bytes < need) {
       if (bb.dev) { cudaStreamSynchronize(c->st); cudaFree(bb.dev); bb.dev = nullptr; bb.bytes = 0; }
       ZQ_CUDA(cudaMalloc(&bb.dev, need));
@@ -599,9 +612,14 @@ int zquatev_refined_device(int n2, double* dD, int ld2, double* deig, void* stre
 int zq_refine_stats(int* iters, double* last_correction, int* fell_back) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return ZQ_ERR_CUDA;
-  if (iters) *iters = g_refine[dev].last_iters;
-  if (last_correction) *last_correction = g_refine[dev].last_emax;
-  if (fell_back) *fell_back = g_refine[dev].last_fallback;
+  Context* c = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    c = g_ctx[dev];
+  }
+  if (iters) *iters = c ? c->rb.last_iters : 0;
+  if (last_correction) *last_correction = c ? c->rb.last_emax : 0.0;
+  if (fell_back) *fell_back = c ? c->rb.last_fallback : 0;
   return ZQ_OK;
 }
 
@@ -645,6 +663,8 @@ int zq_get_block_size(void) { return g_nb; }
 const char* zq_last_error(void) { return last_error_message(); }
 
 int zq_version(void) { return 100; }
+
+long long zq_launch_count(void) { return zq::g_launches.load(std::memory_order_relaxed); }
 
 int zq_release_workspace(void) {
   int dev = 0;

@@ -30,8 +30,10 @@ constexpr int BT = 256;        // threads per CTA
 constexpr int BNMAX = 256;     // largest quaternion order handled in one CTA
 
 struct BatchTask {
-  long long off;    // complex offset of D
-  long long eoff;   // offset of eig
+  long long off;    // complex offset of D (from the launch's D) when Dp is null
+  long long eoff;   // offset of eig (from the launch's eig) when Ep is null
+  double2* Dp;      // or the matrix itself (requests in separate allocations)
+  double* Ep;
   int n, ld;
   int out_slot;     // index into the info array
   int pad;
@@ -51,7 +53,7 @@ struct BatchArgs {
 __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double* ws) {
   const int n = tk.n;
   const int64_t ld = tk.ld;
-  double2* A = a.D + tk.off;
+  double2* A = tk.Dp ? tk.Dp : a.D + tk.off;
   double2* B = A + n;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -283,7 +285,8 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
     XA[r + (int64_t)col * ld] = make_double2(phi[4 * r] * z, phi[4 * r + 1] * z);
     XB[r + (int64_t)col * ld] = make_double2(phi[4 * r + 2] * z, phi[4 * r + 3] * z);
   }
-  for (int k = tid; k < n; k += BT) a.eig[tk.eoff + k] = d[perm[k]];
+  double* eig_out = tk.Ep ? tk.Ep : a.eig + tk.eoff;
+  for (int k = tid; k < n; k += BT) eig_out[k] = d[perm[k]];
   __syncthreads();
   // reflectors backwards: x <- x - w <w,x> - w' [w,x], w' = (-conj(wb), conj(wa))
   for (int j = n - 3; j >= 0; --j) {
@@ -371,7 +374,12 @@ size_t batched_task_bytes() { return sizeof(BatchTask); }
 
 void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot) {
   BatchTask* t = reinterpret_cast<BatchTask*>(dst);
-  t->off = off; t->eoff = eoff; t->n = n; t->ld = ld; t->out_slot = slot; t->pad = 0;
+  t->off = off; t->eoff = eoff; t->Dp = nullptr; t->Ep = nullptr; t->n = n; t->ld = ld; t->out_slot = slot; t->pad = 0;
+}
+
+void batched_fill_task_ptr(void* dst, double2* D, double* eig, int n, int ld, int slot) {
+  BatchTask* t = reinterpret_cast<BatchTask*>(dst);
+  t->off = 0; t->eoff = 0; t->Dp = D; t->Ep = eig; t->n = n; t->ld = ld; t->out_slot = slot; t->pad = 0;
 }
 
 // ----------------------------------------------------------------------------
@@ -444,7 +452,7 @@ extern "C" int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig,
   const long long stride = 12LL * BNMAX + (long long)BNMAX * BNMAX + 64;
   int* info_dev = reinterpret_cast<int*>(scratch + stride);
   BatchTask tk{};
-  tk.off = 0; tk.eoff = 0; tk.n = n2 / 2; tk.ld = ld2; tk.out_slot = 0;
+  tk.off = 0; tk.eoff = 0; tk.Dp = nullptr; tk.Ep = nullptr; tk.n = n2 / 2; tk.ld = ld2; tk.out_slot = 0;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   k_solve_small_noalloc<<<1, BT, 0, st>>>(tk, reinterpret_cast<double2*>(dD), deig, scratch, info_dev);
   ZQ_CUDA(cudaGetLastError());

@@ -118,7 +118,15 @@ enum Status : int {
     }                                                                        \
   } while (0)
 
-#define ZQ_LAUNCH_CHECK() ZQ_CUDA(cudaGetLastError())
+// Every kernel launch of the library is followed by this check, which also
+// counts the launch (zq_launch_count).
+#define ZQ_LAUNCH_CHECK()     \
+  do {                        \
+    zq::count_launch();       \
+    ZQ_CUDA(cudaGetLastError()); \
+  } while (0)
+
+void count_launch();
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line);
 void set_error_message(const char* msg);

@@ -28,6 +28,7 @@
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
+#include <atomic>
 #include <cuda_bf16.h>
 #include <vector>
 
@@ -405,10 +406,16 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   og.m = m; og.n = n; og.ea = ea; og.eb = eb; og.C = g.C; og.ldc = g.ldc;
   og.nsl = nsl; og.lower = opt.structured != 0 ? 1 : 0;
   const int smem = 2 * 3 * OZ_TM * OZ_LDS * (int)sizeof(__nv_bfloat16);
-  static bool attr = false;
-  if (!attr) {
-    ZQ_CUDA(cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    attr = true;
+  {
+    // the shared-memory opt-in is per device; set once for each
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    ZQ_CUDA(cudaGetDevice(&dev));
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+      ZQ_CUDA(cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      attr_set.fetch_or(bit);
+    }
   }
   const int tm = (int)(mp / OZ_TM), tn = (int)(np / OZ_TN);
   dim3 gg = og.lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)tm, (unsigned)tn);
