@@ -42,6 +42,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "n2=8192 solve ms; mixed-stream solves/s, p99 ms vs plain FP64 at resid≤1e-12"
+# DRAM bytes (read + write) per executed bf16 flop of k_oz_gemm, from one ncu capture
+# (n2 = 4096, 8 slices, full tiles: 21.14 GB / 4.95e12 flop)
+OZ_BYTES_PER_FLOP = 21.14e9 / 4.95e12
 
 
 def parse():
@@ -656,7 +659,10 @@ def main():
             "gpu_launches": None,
             "roofline": {"bound": "tensor", "kernel": "k_oz_gemm (bf16 mma.sync, Ozaki slices)",
                          "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                         "frac": (achieved / bf16_peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / bf16_peak) if achieved else None,
+                         "traffic": OZ_BYTES_PER_FLOP * oz_flops / oz_launches if oz_launches else None,
+                         "traffic_source": "profiles/k_oz_gemm_n2-4096.md: dram read+write per executed flop of one "
+                                           "captured launch (n2=4096), scaled by this step's executed flops per launch",
                          "peak_source": peak_src, "launches_per_step": oz_launches, "ms_per_step": oz_ms},
             "stage_ms": {"refine": round(prof["refine"][0] / args.steps, 2), "ozaki": round(oz_ms, 2),
                          "fp32_decomposition": round(ms_step - prof["refine"][0] / args.steps, 2)},
