@@ -136,6 +136,18 @@ extern "C" __global__ void dfma_peak(double* out, int iters, double a, double b)
   }
   out[blockIdx.x*blockDim.x+threadIdx.x] = x0+x1+x2+x3+x4+x5+x6+x7;
 }
+// FP64 on the tensor cores: independent m8n8k4 DMMA chains per warp (512 flops each)
+extern "C" __global__ void dmma_peak(double* out, int iters) {
+  const double a = 1.0 + threadIdx.x * 1e-3, b = 0.5;
+  double c0 = 0, c1 = 0, c2 = 0, c3 = 0, c4 = 0, c5 = 0, c6 = 0, c7 = 0;
+  for (int i = 0; i < iters; ++i) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};" : "+d"(c0), "+d"(c1) : "d"(a), "d"(b));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};" : "+d"(c2), "+d"(c3) : "d"(a), "d"(b));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};" : "+d"(c4), "+d"(c5) : "d"(a), "d"(b));
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};" : "+d"(c6), "+d"(c7) : "d"(a), "d"(b));
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = c0 + c1 + c2 + c3 + c4 + c5 + c6 + c7;
+}
 """
 
 
@@ -156,6 +168,26 @@ def fp64_peak_tflops() -> float:
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         best = max(best, 2.0 * 8 * iters * blocks * threads / (ms * 1e9))
+    return best
+
+
+def dmma_peak_tflops() -> float:
+    """FP64 tensor-core (DMMA m8n8k4) throughput of this GPU (TFLOP/s), CUDA events."""
+    import torch
+
+    lib = _peak_module()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 4, 256, 2048
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.run_dmma(out, blocks, threads, iters)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = max(best, 4.0 * 512.0 * iters * blocks * (threads // 32) / (ms * 1e9))
     return best
 
 
@@ -180,17 +212,26 @@ extern "C" int launch_peak(double* out, int blocks, int threads, int iters, void
   dfma_peak<<<blocks, threads, 0, (cudaStream_t)st>>>(out, iters, 0.999, 1e-3);
   return (int)cudaGetLastError();
 }
+extern "C" int launch_dmma(double* out, int blocks, int threads, int iters, void* st) {
+  dmma_peak<<<blocks, threads, 0, (cudaStream_t)st>>>(out, iters);
+  return (int)cudaGetLastError();
+}
 """)
     so = os.path.join(d, "peak.so")
     subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-shared", "-Xcompiler", "-fPIC",
                     "-cudart", "shared", src, "-o", so], check=True, capture_output=True)
     lib = ctypes.CDLL(so)
     lib.launch_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.launch_dmma.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
 
     class _M:
         @staticmethod
         def run(out, blocks, threads, iters):
             lib.launch_peak(out.data_ptr(), blocks, threads, iters, torch.cuda.current_stream().cuda_stream)
+
+        @staticmethod
+        def run_dmma(out, blocks, threads, iters):
+            lib.launch_dmma(out.data_ptr(), blocks, threads, iters, torch.cuda.current_stream().cuda_stream)
 
     _PEAK_LIB = _M
     return _M
@@ -305,12 +346,9 @@ def batched_case(count: int, fp64_peak: float, seed: int = 2024) -> dict:
     work = torch.empty_like(master)
     deig = torch.zeros(int(ns.sum()), dtype=torch.float64, device="cuda")
 
-    def run():
-        rc = lib.zquatev_batched_device(count, n2s.ctypes.data, n2s.ctypes.data, offs.ctypes.data, eoffs.ctypes.data,
-                                        work.data_ptr(), deig.data_ptr(), st)
-        if rc != 0:
-            raise RuntimeError(f"batched rc={rc}: {_lib.last_error()}")
+    from zquatev_gb300 import solver
 
+    plan = solver.BatchPlan(n2s, n2s, offs, eoffs)  # launch shape tuned on the first run, then graph replays
     times = []
     launches = 0
     for i in range(4):
@@ -319,12 +357,15 @@ def batched_case(count: int, fp64_peak: float, seed: int = 2024) -> dict:
         lc0 = lib.zq_launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        run()
+        plan.run(work, deig)
         e1.record()
         torch.cuda.synchronize()
+        assert plan.info() == 0
         if i >= 1:
             times.append(e0.elapsed_time(e1))
             launches = lib.zq_launch_count() - lc0
+    shape = plan.shape()
+    plan.close()
     ms = float(np.median(times))
     # accuracy on a few of the results (GPU residual)
     from zquatev_gb300 import metrics
@@ -351,6 +392,8 @@ def batched_case(count: int, fp64_peak: float, seed: int = 2024) -> dict:
     del master, work
     return {"workload": f"{count} matrices, n log-uniform in [8, 256] (n2 16..512), random as config 0, per-matrix seeds",
             "ms": ms, "solves_per_s": count / (ms * 1e-3), "gpu_launches": int(launches),
+            "launch": "one CUDA-graph replay of the persistent kernel (zq_batch_plan)",
+            "tuned_shape": shape,
             "fp64_loop_solves_per_s": count / loop_s, "speedup_vs_fp64_loop": loop_s / (ms * 1e-3),
             "fp64_loop_sample": f"{len(sample)} matrices (every 16th), scaled x{count / len(sample):.0f}",
             "algorithmic_tflops": flops / (ms * 1e-3) / 1e12,
@@ -535,6 +578,12 @@ def main():
         if rc != 0:
             raise RuntimeError(f"{fn} rc={rc}: {_lib.last_error()}")
 
+    # panel widths: the project's autotuner at this size, for both precisions
+    tuned_nb = {}
+    for prec in ("fp32", "fp64"):
+        best, ms = solver.autotune_nb(n2, prec)
+        tuned_nb[prec] = {"nb": best, "candidates": {str(c): round(m, 2) for c, m in zip((16, 32, 64), ms)}}
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -650,7 +699,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": f"single quaternion-Hermitian solve n2={n2} (n={n}), random A=(X+X^H)/2, "
                                    "B=(Y-Y^T)/2, complex128, all eigenvectors, drop-in default path (refined)",
-                       "n2": n2, "nb": int(lib.zq_get_block_size()), "parallelism": f"replicas{world}",
+                       "n2": n2, "nb_tuned": tuned_nb, "parallelism": f"replicas{world}",
                        "l2": "inputs (512 MiB left half) larger than L2; restored D2D each step"},
             "fp64_path_ms": fp64_ms,
             "speedup_vs_fp64_path": fp64_ms / ms_step if ms_step > 0 else None,
@@ -667,6 +716,7 @@ def main():
             "stage_ms": {"refine": round(prof["refine"][0] / args.steps, 2), "ozaki": round(oz_ms, 2),
                          "fp32_decomposition": round(ms_step - prof["refine"][0] / args.steps, 2)},
             "fp64_path_roofline": {"pipe": "fp64 DFMA", "peak_tflops_measured": round(fp64_peak, 3),
+                                   "dmma_tflops_measured": round(dmma_peak_tflops(), 3),
                                    "kernels": fp64_roof},
             "accuracy": acc,
             "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": os.cpu_count() or 1, "kind": "port",

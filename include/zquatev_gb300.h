@@ -104,6 +104,37 @@ int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig, void* stre
 int zq_set_block_size(int nb);
 int zq_get_block_size(void);
 
+/* Panel-width autotuner: times the quaternion tridiagonalisation of a seeded
+ * random matrix of order n2 for nb in {16, 32, 64} and stores the fastest for
+ * n2's size bucket (powers of two of n) and precision (0: FP64 path, 1: FP32
+ * decomposition of the refined path); later solves of that bucket use it.
+ * best_nb receives the choice, ms (3 doubles, may be NULL) the timings. The
+ * reference hard-codes nb = 20 (zquatev.cc:64); nb = 128 is not offered (the
+ * panel kernels hold at most 64 reflectors). zq_set_block_size clears the table. */
+int zq_autotune_nb(int n2, int precision, int* best_nb, double* ms);
+/* Tuned width for n2's bucket (0 = not tuned), and setting it directly (e.g.
+ * from a saved table; 0 clears). */
+int zq_tuned_nb(int n2, int precision);
+int zq_set_tuned_nb(int n2, int precision, int nb);
+
+/* Batch plan: one layout of small matrices (every n2 <= 512; arguments as
+ * zquatev_batched_device) solved repeatedly. Tasks are ordered largest first
+ * and uploaded once. ctas_per_sm 1..4 fixes the persistent kernel's launch
+ * shape; 0 lets the first run choose it by timing each candidate on the
+ * caller's batch (the input is restored between candidates). The launch is
+ * captured in a CUDA graph; each run replays it on `stream` without
+ * synchronising (recaptured when dD or deig change). zq_batch_plan_info waits
+ * for `stream` and returns the largest per-matrix info. No counterpart in the
+ * reference. */
+typedef struct zq_batch_plan zq_batch_plan;
+zq_batch_plan* zq_batch_plan_create(int count, const int* n2s, const int* ld2s, const long long* offs,
+                                    const long long* eoffs, int ctas_per_sm);
+int zq_batch_plan_run(zq_batch_plan* p, double* dD, double* deig, void* stream);
+int zq_batch_plan_info(zq_batch_plan* p, void* stream);
+/* Chosen CTAs per SM, CTAs of the captured launch, and the tuning times (4 doubles, ms; 0 = not tried). */
+int zq_batch_plan_shape(zq_batch_plan* p, int* ctas_per_sm, int* ctas, double* tune_ms);
+int zq_batch_plan_destroy(zq_batch_plan* p);
+
 /* Kernel-class timing with CUDA events on the launching streams (for the
  * benchmark's roofline figures; off by default, adds two event records per
  * bracketed launch). Classes: 0 quaternion hemv, 1 trailing update, 2 panel
@@ -132,11 +163,11 @@ int zq_release_workspace(void);
  * arrival order while the admitted footprints fit hbm_budget_bytes (<= 0:
  * 80% of the free device memory at creation). An admitted request's matrix is
  * copied to the device at once and stays there until its result is copied
- * back into D and eig. Requests with n2 <= 512 are solved together in
- * launches of the persistent batched kernel (every one that is ready when a
- * batch slot frees up, at most max_batch); larger ones run on `lanes`
- * concurrent lanes through the drop-in's default path (refined, FP64
- * fallback). D and eig must stay valid until zq_server_wait returns for the
+ * back into D and eig. Requests with n2 <= batch_max_n2 (at most 512) are
+ * solved together in launches of the persistent batched kernel (every one that
+ * is ready when a batch slot frees up, at most max_batch); larger ones run on
+ * `lanes` concurrent lanes through the drop-in's default path (refined above
+ * n2 = 512, FP64 below; FP64 fallback). D and eig must stay valid until zq_server_wait returns for the
  * request. No counterpart in the reference. */
 typedef struct zq_server zq_server;
 typedef struct zq_server_stats {
@@ -160,7 +191,7 @@ typedef struct zq_server_stats {
 long long zq_solve_footprint(int n2, int path);
 
 /* NULL on failure (zq_last_error). */
-zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch);
+zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch, int batch_max_n2);
 /* Request id (>= 0), or a negative code: argument errors as zquatev_c, -103 if
  * the footprint can never fit the budget. */
 long long zq_server_submit(zq_server* s, int n2, double* D, int ld2, double* eig);

@@ -49,7 +49,7 @@ def _check(d, out, eig):
 
 def test_mix_equals_alone(gpu):
     mats = _mix()
-    with Server(lanes=4) as srv:
+    with Server(lanes=4, batch_max_n2=512) as srv:
         alone = []
         for d in mats:
             out, eig = _copy(d), np.zeros(d.shape[1])
@@ -73,15 +73,21 @@ def test_mix_equals_alone(gpu):
         assert metrics.subspace_distance(out, eig[:n], aout, aeig[:n], tol) < 1e-8
 
 
-def test_routing_and_timestamps(gpu):
+@pytest.mark.parametrize("batch_max_n2", [512, 128, 0])
+def test_routing_and_timestamps(gpu, batch_max_n2):
     mats = _mix()
-    with Server(lanes=2) as srv:
+    with Server(lanes=2, batch_max_n2=batch_max_n2) as srv:
         outs = [(_copy(d), np.zeros(d.shape[1])) for d in mats]
         ids = [srv.submit(d.shape[1], o, d.shape[0], e) for d, (o, e) in zip(mats, outs)]
         res = [srv.wait(i) for i in ids]
     for n, (info, t) in zip(SIZES, res):
         assert info == 0
-        assert t["path"] == ("batched" if n <= 256 else "refined")
+        if 2 * n <= batch_max_n2:
+            assert t["path"] == "batched"
+        elif n >= 256:
+            assert t["path"] in ("refined", "refined->fp64")
+        else:
+            assert t["path"] == "fp64"
         assert t["submit"] <= t["admit"] <= t["start"] <= t["done"]
 
 

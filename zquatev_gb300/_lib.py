@@ -40,7 +40,15 @@ SIGNATURES = {
     "zq_version": (_c_int, []),
     "zq_launch_count": (_c_ll, []),
     "zq_solve_footprint": (_c_ll, [_c_int, _c_int]),
-    "zq_server_create": (_vp, [_c_ll, _c_int, _c_int]),
+    "zq_autotune_nb": (_c_int, [_c_int, _c_int, _vp, _vp]),
+    "zq_tuned_nb": (_c_int, [_c_int, _c_int]),
+    "zq_set_tuned_nb": (_c_int, [_c_int, _c_int, _c_int]),
+    "zq_batch_plan_create": (_vp, [_c_int, _vp, _vp, _vp, _vp, _c_int]),
+    "zq_batch_plan_run": (_c_int, [_vp, _vp, _vp, _vp]),
+    "zq_batch_plan_info": (_c_int, [_vp, _vp]),
+    "zq_batch_plan_shape": (_c_int, [_vp, _vp, _vp, _vp]),
+    "zq_batch_plan_destroy": (_c_int, [_vp]),
+    "zq_server_create": (_vp, [_c_ll, _c_int, _c_int, _c_int]),
     "zq_server_submit": (_c_ll, [_vp, _c_int, _vp, _c_int, _vp]),
     "zq_server_test": (_c_int, [_vp, _c_ll]),
     "zq_server_wait": (_c_int, [_vp, _c_ll, _vp, _vp]),

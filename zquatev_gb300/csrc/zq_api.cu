@@ -36,7 +36,7 @@ namespace zq {
 static thread_local std::string g_last_error;
 
 static std::atomic<long long> g_launches{0};
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launch(int k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line) {
   char buf[512];
@@ -109,9 +109,16 @@ static Context* g_ctx[64];
 static int g_nb = 32;   // panel width (autotuned table may override per n)
 static int g_nbq = 64;  // Q-formation block
 
-static int nb_for(int n) {
+// Panel width per precision (0 FP64 path, 1 FP32 decomposition of the refined
+// path) and size bucket floor(log2 n), filled by zq_autotune_nb; 0 = default.
+static std::atomic<int> g_nb_table[2][32];
+static int nb_bucket(int n) { int b = 0; while ((2 << b) <= n && b < 31) ++b; return b; }
+void nb_table_set(int prec, int n, int nb) { g_nb_table[prec & 1][nb_bucket(n)].store(nb); }
+int nb_table_get(int prec, int n) { return g_nb_table[prec & 1][nb_bucket(n)].load(); }
+
+static int nb_for(int n, int prec = 0) {
   if (const char* s = getenv("ZQ_NB")) { const int v = atoi(s); if (v >= 1 && v <= 64) return v; }
-  (void)n;
+  if (const int t = nb_table_get(prec, n)) return t;
   return g_nb;
 }
 
@@ -393,7 +400,7 @@ int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cu
   ra.ows_bytes = (mode == 1) ? ozaki_workspace_bytes(n) : 0;
   ra.dc = &c->dc;
   ra.fdesc = reinterpret_cast<DgemmDescT<float>*>(desc1);
-  ra.nb = nb_for(n); ra.nbq = g_nbq; ra.mode = mode;
+  ra.nb = nb_for(n, 1); ra.nbq = g_nbq; ra.mode = mode;
   ra.max_iter = 6;
   ra.tol = 1e-7;   // the update squares the error: |E| <= 1e-7 leaves ~1e-14
   ra.cluster_tol = 1e-13;
@@ -655,6 +662,8 @@ int zq_profile_flops(int cls, double* flops) {
 int zq_set_block_size(int nb) {
   if (nb < 1 || nb > 64) { set_msg("block size must be in [1, 64]"); return ZQ_ERR_ARG; }
   g_nb = nb;
+  for (auto& row : g_nb_table)
+    for (auto& v : row) v.store(0);  // an explicit width replaces the tuned table
   return ZQ_OK;
 }
 

@@ -126,7 +126,7 @@ enum Status : int {
     ZQ_CUDA(cudaGetLastError()); \
   } while (0)
 
-void count_launch();
+void count_launch(int k = 1);
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line);
 void set_error_message(const char* msg);

@@ -60,6 +60,9 @@ int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool
 int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cudaStream_t st, int mode);
 // drop-in policy: 0 FP64 path, 1 refined path for quaternion size n
 int path_for(int n);
+// tuned panel widths (prec 0: FP64 path, 1: FP32 decomposition), 0 = not tuned
+void nb_table_set(int prec, int n, int nb);
+int nb_table_get(int prec, int n);
 
 // batched kernel (zq_batched.cu)
 long long batched_ws_stride();

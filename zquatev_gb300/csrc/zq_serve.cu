@@ -9,7 +9,7 @@
 // stays there until its result is copied back.
 //
 // Admitted requests run as soon as an execution slot is free:
-//  * n <= 256 (n2 <= 512): batch workers take every such request that is ready
+//  * n2 <= batch_max_n2 (at most 512): batch workers take every such request that is ready
 //    when they become free and solve them in one launch of the persistent
 //    batched kernel (largest first), so the batch size follows the load;
 //  * larger ones: lane workers (one host thread, stream pair and context each)
@@ -68,6 +68,7 @@ struct zq_server {
   std::chrono::steady_clock::time_point t0;
   size_t budget = 0;
   int max_batch = 0;
+  int batch_max_n = 0;                // requests with n <= this go to the batched kernel
   std::mutex mu;
   std::condition_variable cv_admit, cv_lane, cv_batch, cv_done;
   std::deque<zq::Req*> pending, ready_lane, ready_small;
@@ -292,10 +293,13 @@ long long zq_solve_footprint(int n2, int path) {
   return (long long)(mat + f + (path == 1 ? r : 0));
 }
 
-zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch) {
+zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch, int batch_max_n2) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) { set_error_message("no CUDA device"); return nullptr; }
-  if (lanes < 1 || lanes > 64 || max_batch < 1) { set_error_message("lanes must be 1..64, max_batch >= 1"); return nullptr; }
+  if (lanes < 1 || lanes > 64 || max_batch < 1 || batch_max_n2 < 0 || batch_max_n2 > 2 * batched_max_n()) {
+    set_error_message("lanes must be 1..64, max_batch >= 1, batch_max_n2 in [0, 512]");
+    return nullptr;
+  }
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { set_error_message("cudaMemGetInfo failed"); return nullptr; }
   Server* s = new Server();
@@ -303,6 +307,7 @@ zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch
   s->t0 = Clock::now();
   s->budget = hbm_budget_bytes > 0 ? (size_t)hbm_budget_bytes : (size_t)(0.8 * (double)free_b);
   s->max_batch = max_batch;
+  s->batch_max_n = batch_max_n2 / 2;
   cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
   // keep freed request memory in the stream-ordered pool between requests
   cudaMemPool_t pool;
@@ -344,7 +349,7 @@ long long zq_server_submit(zq_server* s, int n2, double* D, int ld2, double* eig
   r->n2 = n2; r->ld2 = ld2; r->n = n2 / 2;
   r->hD = reinterpret_cast<double2*>(D);
   r->heig = eig;
-  r->small = r->n <= batched_max_n();
+  r->small = r->n <= s->batch_max_n;
   r->mat_bytes = sizeof(double2) * (size_t)n2 * n2 + sizeof(double) * (size_t)(r->n + 32);
   if (r->small) {
     r->footprint = (size_t)zq_solve_footprint(n2, 2);

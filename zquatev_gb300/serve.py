@@ -21,9 +21,9 @@ PATHS = {0: "fp64", 1: "refined", 2: "batched", 3: "refined->fp64"}
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes: int = 0, lanes: int = 4, max_batch: int = 4096):
+    def __init__(self, hbm_budget_bytes: int = 0, lanes: int = 4, max_batch: int = 4096, batch_max_n2: int = 128):
         self._lib = _lib.load()
-        self._h = self._lib.zq_server_create(int(hbm_budget_bytes), int(lanes), int(max_batch))
+        self._h = self._lib.zq_server_create(int(hbm_budget_bytes), int(lanes), int(max_batch), int(batch_max_n2))
         if not self._h:
             raise _lib.ZquatevError(f"zq_server_create failed: {_lib.last_error()}")
         self._live: dict[int, tuple[np.ndarray, np.ndarray]] = {}

@@ -92,3 +92,72 @@ def stedc_device(d, e, lam, z, stream=None) -> int:
     st = stream if stream is not None else torch.cuda.current_stream(d.device)
     return _lib.load().zq_stedc_device(n, d.data_ptr(), e.data_ptr() if n > 1 else 0, lam.data_ptr(),
                                        z.data_ptr(), n, st.cuda_stream)
+
+
+# ------------------------------------------------------------------- tuning
+def autotune_nb(n2: int, precision: str = "fp64") -> tuple[int, list[float]]:
+    """Times the tridiagonalisation at order n2 for panel widths 16, 32, 64 and
+    stores the fastest for n2's size bucket ("fp64": plain path, "fp32": the
+    refined path's decomposition). Returns (best nb, [ms per candidate])."""
+    import ctypes
+
+    best = ctypes.c_int()
+    ms = (ctypes.c_double * 3)()
+    prec = {"fp64": 0, "fp32": 1}[precision]
+    _lib.check(_lib.load().zq_autotune_nb(n2, prec, ctypes.byref(best), ms), "zq_autotune_nb")
+    return best.value, list(ms)
+
+
+class BatchPlan:
+    """Graph-captured batched solve of one layout of small matrices (n2 <= 512).
+
+    Arguments as zquatev_batched_device: per-matrix n2, ld2, complex offset of
+    each matrix in the device buffer and offset of its eigenvalues. With
+    ctas_per_sm = 0 the first run picks the launch shape by timing each
+    candidate on the caller's batch.
+    """
+
+    def __init__(self, n2s, ld2s, offs, eoffs, ctas_per_sm: int = 0):
+        self._n2s = np.ascontiguousarray(n2s, dtype=np.int32)
+        self._ld2s = np.ascontiguousarray(ld2s, dtype=np.int32)
+        self._offs = np.ascontiguousarray(offs, dtype=np.int64)
+        self._eoffs = np.ascontiguousarray(eoffs, dtype=np.int64)
+        lib = _lib.load()
+        self._h = lib.zq_batch_plan_create(self._n2s.size, self._n2s.ctypes.data, self._ld2s.ctypes.data,
+                                           self._offs.ctypes.data, self._eoffs.ctypes.data, ctas_per_sm)
+        if not self._h:
+            raise _lib.ZquatevError(f"zq_batch_plan_create failed: {_lib.last_error()}")
+
+    def run(self, dmat, deig, stream=None) -> None:
+        """dmat: complex128 CUDA tensor holding the batch; deig: float64 CUDA tensor."""
+        import torch
+
+        st = stream if stream is not None else torch.cuda.current_stream(dmat.device)
+        _lib.check(_lib.load().zq_batch_plan_run(self._h, dmat.data_ptr(), deig.data_ptr(), st.cuda_stream),
+                   "zq_batch_plan_run")
+
+    def info(self, stream=None) -> int:
+        import torch
+
+        st = stream if stream is not None else torch.cuda.current_stream()
+        return _lib.check(_lib.load().zq_batch_plan_info(self._h, st.cuda_stream), "zq_batch_plan_info")
+
+    def shape(self) -> dict:
+        import ctypes
+
+        cps, ctas = ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_double * 4)()
+        _lib.check(_lib.load().zq_batch_plan_shape(self._h, ctypes.byref(cps), ctypes.byref(ctas), ms),
+                   "zq_batch_plan_shape")
+        return {"ctas_per_sm": cps.value, "ctas": ctas.value, "tune_ms": list(ms)}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().zq_batch_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
