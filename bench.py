@@ -42,9 +42,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "n2=8192 solve ms; mixed-stream solves/s, p99 ms vs plain FP64 at resid≤1e-12"
-# DRAM bytes (read + write) per executed bf16 flop of k_oz_gemm, from one ncu capture
-# (n2 = 4096, 8 slices, full tiles: 21.14 GB / 4.95e12 flop)
-OZ_BYTES_PER_FLOP = 21.14e9 / 4.95e12
+# DRAM bytes (read + write) per executed bf16 flop of the Ozaki product kernel,
+# from one ncu capture of k_oz_umma (None until captured)
+OZ_BYTES_PER_FLOP = None
 
 
 def parse():
@@ -706,10 +706,11 @@ def main():
             "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": n2 * n * 16,
                     "d2h_bytes_per_step": n2 * n2 * 16 + n * 8},
             "gpu_launches": None,
-            "roofline": {"bound": "tensor", "kernel": "k_oz_gemm (bf16 mma.sync, Ozaki slices)",
+            "roofline": {"bound": "tensor", "kernel": "k_oz_umma (bf16 tcgen05.mma, TMEM accumulators, TMA; Ozaki slices)",
                          "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": (achieved / bf16_peak) if achieved else None,
-                         "traffic": OZ_BYTES_PER_FLOP * oz_flops / oz_launches if oz_launches else None,
+                         "traffic": (OZ_BYTES_PER_FLOP * oz_flops / oz_launches
+                                     if (oz_launches and OZ_BYTES_PER_FLOP) else None),
                          "traffic_source": "profiles/k_oz_gemm_n2-4096.md: dram read+write per executed flop of one "
                                            "captured launch (n2=4096), scaled by this step's executed flops per launch",
                          "peak_source": peak_src, "launches_per_step": oz_launches, "ms_per_step": oz_ms},

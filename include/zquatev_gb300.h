@@ -10,7 +10,8 @@
  *
  * Return codes: 0 success; -1 bad n2 (odd or negative); -2 null D; -3 ld2 < n2;
  * -4 null eig; -5 other bad argument; -100 CUDA failure; -101 out of device
- * memory; -103 size above the fixed limit of the called entry point.
+ * memory; -103 size above the fixed limit of the called entry point; -104 a
+ * device-side pipeline wait ran out of time (the kernel stopped and said so).
  * zq_last_error() describes the last failure on the calling thread.
  */
 #ifndef ZQUATEV_GB300_H
@@ -103,6 +104,13 @@ int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig, void* stre
  * nb = 20 at zquatev.cc:64). Valid range 1..64; default 32. */
 int zq_set_block_size(int nb);
 int zq_get_block_size(void);
+
+/* Tensor-core kernel of the Ozaki products in the refined path and
+ * zq_zgemm_accurate: 0 = mma.sync (bf16 m16n8k16, 64 x 64 tiles), 1 = tcgen05
+ * (TMEM accumulators, TMA-fed 128 x 256 MMAs; the default). Same arithmetic
+ * and results. */
+int zq_set_ozaki_kernel(int which);
+int zq_get_ozaki_kernel(void);
 
 /* Panel-width autotuner: times the quaternion tridiagonalisation of a seeded
  * random matrix of order n2 for nb in {16, 32, 64} and stores the fastest for

@@ -41,13 +41,15 @@ def test_refined_random(gpu, n, mode):
     assert np.all(np.diff(eig[:n]) >= 0)
 
 
-@pytest.mark.parametrize("opa,opb", [(2, 0), (1, 0), (0, 0), (0, 3)])
-def test_accurate_zgemm(gpu, opa, opb):
-    """The Ozaki tensor-core product agrees with an extended-precision product to ~1e-15 relative."""
+@pytest.mark.parametrize("kernel", [0, 1], ids=["mma_sync", "tcgen05"])
+@pytest.mark.parametrize("opa,opb,m,n,k", [(2, 0, 70, 50, 300), (1, 0, 70, 50, 300), (0, 0, 70, 50, 300),
+                                           (0, 3, 70, 50, 300), (0, 0, 128, 128, 32), (2, 0, 300, 260, 700)])
+def test_accurate_zgemm(gpu, kernel, opa, opb, m, n, k):
+    """The Ozaki tensor-core product (either kernel) agrees with an extended-precision product to ~1e-15 relative."""
     import torch
 
-    rng = np.random.default_rng(opa * 10 + opb)
-    m, n, k = 70, 50, 300
+    assert gpu.zq_set_ozaki_kernel(kernel) == 0
+    rng = np.random.default_rng(opa * 10 + opb + m)
     ash = (k, m) if opa in (1, 2) else (m, k)
     bsh = (n, k) if opb in (1, 2) else (k, n)
     a = rng.standard_normal(ash) + 1j * rng.standard_normal(ash)
@@ -66,6 +68,28 @@ def test_accurate_zgemm(gpu, opa, opb):
     torch.cuda.synchronize()
     assert rc == 0, _lib.last_error()
     c = dc.cpu().numpy().T
+    gpu.zq_set_ozaki_kernel(1)
     scale = np.abs(op(a, opa)) @ np.abs(op(b, opb))
     err = np.abs(c - exact.astype(np.complex128)) / scale
     assert err.max() < 2e-15
+
+
+@pytest.fixture
+def mma_sync(gpu):
+    assert gpu.zq_set_ozaki_kernel(0) == 0
+    yield gpu
+    gpu.zq_set_ozaki_kernel(1)
+
+
+@pytest.mark.parametrize("n", [5, 64, 300, 700])
+def test_refined_mma_sync_products(mma_sync, n):
+    """The refined path with its Ozaki products on the mma.sync kernel meets the same bar."""
+    d = inputs.random_matrix(n, 6100 + n)
+    out, eig = refined(mma_sync, d, 1)
+    h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
+    ref = np.linalg.eigvalsh(h)[::2]
+    hn = metrics.h_norm2(ref)
+    assert metrics.eig_error(eig[:n], ref, hn) <= TOL
+    assert metrics.residual(h, out, eig[:n]) <= TOL
+    assert metrics.orthonormality(out) <= TOL
+    assert metrics.structure_exact(out, n)

@@ -41,6 +41,8 @@ SIGNATURES = {
     "zq_launch_count": (_c_ll, []),
     "zq_solve_footprint": (_c_ll, [_c_int, _c_int]),
     "zq_autotune_nb": (_c_int, [_c_int, _c_int, _vp, _vp]),
+    "zq_set_ozaki_kernel": (_c_int, [_c_int]),
+    "zq_get_ozaki_kernel": (_c_int, []),
     "zq_tuned_nb": (_c_int, [_c_int, _c_int]),
     "zq_set_tuned_nb": (_c_int, [_c_int, _c_int, _c_int]),
     "zq_batch_plan_create": (_vp, [_c_int, _vp, _vp, _vp, _vp, _c_int]),

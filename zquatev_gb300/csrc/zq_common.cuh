@@ -107,6 +107,7 @@ enum Status : int {
   ZQ_ERR_NOMEM = -101,  // device allocation failed
   ZQ_ERR_NOTFINITE = -102,  // input contains Inf/NaN
   ZQ_ERR_LIMIT = -103,  // size above a fixed limit of the called entry point
+  ZQ_ERR_TIMEOUT = -104,  // a device-side wait ran out of time (the kernel stopped and reported it)
 };
 
 #define ZQ_CUDA(call)                                                        \

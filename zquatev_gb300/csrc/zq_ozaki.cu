@@ -22,13 +22,17 @@
 // With S = 7 the dropped terms are below 2^-49 of sigma_i tau_j per product,
 // i.e. FP64-level accuracy for the refinement's sums.
 //
-// The product kernel is a bf16 mma.sync (m16n8k16) tiled GEMM: 64x64 CTA
-// tile, four 32x32 warp tiles computing the real and imaginary outputs from one
-// staged A tile and two B tiles, cp.async double buffering.
+// Two product kernels with the same arithmetic: k_oz_umma (zq_ozaki_umma.cu,
+// tcgen05 MMAs into TMEM fed by TMA; the default) and k_oz_gemm below, a bf16
+// mma.sync (m16n8k16) tiled GEMM: 64x64 CTA tile, four 32x32 warp tiles
+// computing the real and imaginary outputs from one staged A tile and two B
+// tiles, cp.async double buffering.
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
 #include <atomic>
+#include <cstdlib>
+#include <cstring>
 #include <cuda_bf16.h>
 #include <vector>
 
@@ -41,6 +45,7 @@ constexpr int OZ_SUPER = 64 * 1024;      // terms per int32 partial (64 * 1024 *
 constexpr int OZ_TM = 64, OZ_TN = 64, OZ_TK = 64;
 constexpr int OZ_LDS = OZ_TK + 8;        // padded shared row (bf16), 144 bytes
 constexpr int OZ_THREADS = 128;
+constexpr int OZ_PAD = 128;             // slice rows padded for either product kernel
 
 // element (r, c) of op(X)
 __device__ __forceinline__ double2 oz_op(const double2* X, int64_t ld, int op, int r, int c) {
@@ -317,14 +322,32 @@ __global__ void __launch_bounds__(OZ_THREADS, 3) k_oz_gemm(OzGemmArgs g) {
 
 static int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
+// product kernel: 0 mma.sync (k_oz_gemm), 1 tcgen05 (k_oz_umma)
+static std::atomic<int> g_oz_kernel{1};
+int ozaki_kernel() {
+  if (const char* s = getenv("ZQ_OZAKI")) {
+    if (!strcmp(s, "mma")) return 0;
+    if (!strcmp(s, "umma")) return 1;
+  }
+  return g_oz_kernel.load();
+}
+int set_ozaki_kernel(int k) {
+  if (k != 0 && k != 1) return ZQ_ERR_ARG;
+  g_oz_kernel.store(k);
+  return ZQ_OK;
+}
+int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_bfloat16* Bis, int mp, int np, int Kp,
+                 int m, int n, int nsl, int lower, const int* ea, const int* eb, double2* C, int64_t ldc, int* err,
+                 cudaStream_t st);
+
 // workspace for products with m, n <= 2 * nq and Kp <= 4 * nq + 64
 size_t ozaki_workspace_bytes(int nq) {
-  const int64_t mp = rup(2 * (int64_t)nq, 64), np = rup(2 * (int64_t)nq, 64), Kp = rup(4 * (int64_t)nq, 64);
+  const int64_t mp = rup(2 * (int64_t)nq, OZ_PAD), np = rup(2 * (int64_t)nq, OZ_PAD), Kp = rup(4 * (int64_t)nq, 64);
   size_t b = 0;
   b += sizeof(__nv_bfloat16) * (size_t)OZ_SMAX * mp * Kp;       // A slices
   b += sizeof(__nv_bfloat16) * (size_t)OZ_SMAX * np * Kp * 2;   // B slices (re / im forms)
   b += sizeof(int) * (size_t)(mp + np + 64);
-  return b + 8 * 256;
+  return b + 9 * 256;
 }
 
 // structured square outputs: fill the upper triangle from the lower one
@@ -370,9 +393,9 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   b.X1 = g.B1; b.ld1 = g.ldb1; b.op1 = opb1; b.K1 = g.k1;
   b.X2 = two ? g.B2 : nullptr; b.ld2 = g.ldb2; b.op2 = opb2; b.K2 = two ? g.k2 : 0; b.s2 = 1.0;
   const int64_t Kp = rup(2 * ((int64_t)g.k1 + (two ? g.k2 : 0)), OZ_TK);
-  const int64_t mp = rup(m, OZ_TM), np = rup(n, OZ_TN);
+  const int64_t mp = rup(m, OZ_PAD), np = rup(n, OZ_PAD);
   size_t need = sizeof(__nv_bfloat16) * ((size_t)OZ_SMAX * mp * Kp + 2 * (size_t)OZ_SMAX * np * Kp) +
-                sizeof(int) * (size_t)(mp + np + 64) + 8 * 256;
+                sizeof(int) * (size_t)(mp + np + 64) + 9 * 256;
   if (need > ws_bytes) { set_error_message("zgemm_ozaki: workspace too small"); return ZQ_ERR_LIMIT; }
   if (g.alpha.x != 1.0 || g.alpha.y != 0.0 || g.beta.x != 0.0 || g.beta.y != 0.0) {
     set_error_message("zgemm_ozaki: only C = op(A) op(B) (alpha 1, beta 0)");
@@ -389,6 +412,7 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   __nv_bfloat16* Bis = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * OZ_SMAX * np * Kp));
   int* ea = reinterpret_cast<int*>(take(sizeof(int) * mp));
   int* eb = reinterpret_cast<int*>(take(sizeof(int) * np));
+  int* errf = reinterpret_cast<int*>(take(sizeof(int) * 4));
   auto grid = [](int64_t total) { int64_t x = (total + 255) / 256; return (int)(x > 16384 ? 16384 : x); };
   if (!opt.reuse_a) {
     k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
@@ -405,30 +429,51 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   og.mp = (int)mp; og.np = (int)np; og.Kp = (int)Kp;
   og.m = m; og.n = n; og.ea = ea; og.eb = eb; og.C = g.C; og.ldc = g.ldc;
   og.nsl = nsl; og.lower = opt.structured != 0 ? 1 : 0;
-  const int smem = 2 * 3 * OZ_TM * OZ_LDS * (int)sizeof(__nv_bfloat16);
-  {
-    // the shared-memory opt-in is per device; set once for each
-    static std::atomic<unsigned long long> attr_set{0};
-    int dev = 0;
-    ZQ_CUDA(cudaGetDevice(&dev));
-    const unsigned long long bit = 1ull << (dev & 63);
-    if (!(attr_set.load() & bit)) {
-      ZQ_CUDA(cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-      attr_set.fetch_or(bit);
-    }
-  }
-  const int tm = (int)(mp / OZ_TM), tn = (int)(np / OZ_TN);
-  dim3 gg = og.lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)tm, (unsigned)tn);
-  {
-    // executed tensor-core flops: slice pairs x (Re, Im) x tiles x 64 x 64 x Kp x 2
+  const bool lower = og.lower != 0;
+  if (ozaki_kernel() == 1) {
+    // tcgen05 / TMEM / TMA product (zq_ozaki_umma.cu), 128 x 128 tiles
+    const int tm = (int)(mp / 128), tn = (int)(np / 128);
     const double pairs = (double)nsl * (nsl + 1) / 2.0;
-    const double tiles = og.lower ? (double)tm * (tm + 1) / 2.0 : (double)tm * tn;
-    prof_add_flops(PC_OZAKI, pairs * 2.0 * tiles * OZ_TM * OZ_TN * (double)Kp * 2.0);
+    const double tiles = lower ? (double)tm * (tm + 1) / 2.0 : (double)tm * tn;
+    prof_add_flops(PC_OZAKI, pairs * 2.0 * tiles * 128.0 * 128.0 * (double)Kp * 2.0);
+    prof_begin(PC_OZAKI, st);
+    if (int rc = oz_umma_gemm(As, Brs, Bis, (int)mp, (int)np, (int)Kp, m, n, nsl, lower ? 1 : 0, ea, eb, g.C, g.ldc, errf,
+                              st))
+      return rc;
+    prof_end(PC_OZAKI, st);
+    int herr = 0;
+    ZQ_CUDA(cudaMemcpyAsync(&herr, errf, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ZQ_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+      set_error_message("k_oz_umma: a pipeline wait ran out of time (kernel stopped)");
+      return ZQ_ERR_TIMEOUT;
+    }
+  } else {
+    const int smem = 2 * 3 * OZ_TM * OZ_LDS * (int)sizeof(__nv_bfloat16);
+    {
+      // the shared-memory opt-in is per device; set once for each
+      static std::atomic<unsigned long long> attr_set{0};
+      int dev = 0;
+      ZQ_CUDA(cudaGetDevice(&dev));
+      const unsigned long long bit = 1ull << (dev & 63);
+      if (!(attr_set.load() & bit)) {
+        ZQ_CUDA(cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr_set.fetch_or(bit);
+      }
+    }
+    const int tm = (int)((m + OZ_TM - 1) / OZ_TM), tn = (int)((n + OZ_TN - 1) / OZ_TN);
+    dim3 gg = og.lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)tm, (unsigned)tn);
+    {
+      // executed tensor-core flops: slice pairs x (Re, Im) x tiles x 64 x 64 x Kp x 2
+      const double pairs = (double)nsl * (nsl + 1) / 2.0;
+      const double tiles = og.lower ? (double)tm * (tm + 1) / 2.0 : (double)tm * tn;
+      prof_add_flops(PC_OZAKI, pairs * 2.0 * tiles * OZ_TM * OZ_TN * (double)Kp * 2.0);
+    }
+    prof_begin(PC_OZAKI, st);
+    k_oz_gemm<<<gg, OZ_THREADS, smem, st>>>(og);
+    prof_end(PC_OZAKI, st);
+    ZQ_LAUNCH_CHECK();
   }
-  prof_begin(PC_OZAKI, st);
-  k_oz_gemm<<<gg, OZ_THREADS, smem, st>>>(og);
-  prof_end(PC_OZAKI, st);
-  ZQ_LAUNCH_CHECK();
   if (opt.structured != 0) {
     k_oz_symfill<<<grid((int64_t)m * n), 256, 0, st>>>(g.C, g.ldc, m, opt.structured);
     ZQ_LAUNCH_CHECK();
@@ -437,6 +482,12 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
 }
 
 }  // namespace zq
+
+extern "C" int zq_set_ozaki_kernel(int which) {
+  if (zq::set_ozaki_kernel(which)) { zq::set_error_message("kernel must be 0 (mma.sync) or 1 (tcgen05)"); return zq::ZQ_ERR_ARG; }
+  return zq::ZQ_OK;
+}
+extern "C" int zq_get_ozaki_kernel(void) { return zq::ozaki_kernel(); }
 
 // Public utility: FP64-accurate complex product on the tensor cores.
 //   C = op(A) op(B) (m x n, K inner), op codes 0 N, 1 T, 2 C (conj-transpose), 3 R (conj)
