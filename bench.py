@@ -43,8 +43,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "n2=8192 solve ms; mixed-stream solves/s, p99 ms vs plain FP64 at resid≤1e-12"
 # DRAM bytes (read + write) per executed bf16 flop of the Ozaki product kernel,
-# from one ncu capture of k_oz_umma (None until captured)
-OZ_BYTES_PER_FLOP = None
+# from one ncu capture of k_oz_umma (n2 = 4096, 8 slices: 4.284 GB / 2.63e12 flop)
+OZ_BYTES_PER_FLOP = 4.284e9 / 2.63e12
 
 
 def parse():
@@ -711,7 +711,7 @@ def main():
                          "frac": (achieved / bf16_peak) if achieved else None,
                          "traffic": (OZ_BYTES_PER_FLOP * oz_flops / oz_launches
                                      if (oz_launches and OZ_BYTES_PER_FLOP) else None),
-                         "traffic_source": "profiles/k_oz_gemm_n2-4096.md: dram read+write per executed flop of one "
+                         "traffic_source": "profiles/k_oz_umma_n2-4096.md: dram read+write per executed flop of one "
                                            "captured launch (n2=4096), scaled by this step's executed flops per launch",
                          "peak_source": peak_src, "launches_per_step": oz_launches, "ms_per_step": oz_ms},
             "stage_ms": {"refine": round(prof["refine"][0] / args.steps, 2), "ozaki": round(oz_ms, 2),

@@ -188,7 +188,7 @@ static Layout layout_for(int n, int nbmax, int nbq, size_t nnodes, size_t ndescs
   L.dc = align256(sizeof(double) * DcPlan::workspace_doubles(n));
   L.fq = align256(form_q_workspace_bytes(n, nbq));
   L.nodes = align256(sizeof(DcNode) * (nnodes + 1));
-  L.descs = align256(sizeof(DgemmDesc) * (ndescs + 2));
+  L.descs = align256(DcPlan::desc_bytes(ndescs));
   L.total = L.tri + L.small + L.dc + L.fq + L.nodes + L.descs;
   return L;
 }
@@ -408,6 +408,9 @@ int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cu
   if (const char* s = getenv("ZQ_REFINE_MAXIT")) ra.max_iter = atoi(s);
   if (const char* s = getenv("ZQ_REFINE_EPS")) { const double v = atof(s); if (v > 0.0 && v < 0.5) ra.pair_eps = v; }
   ra.st = c->st;
+  ra.st2 = c->st2;
+  ra.ev_fork = c->ev_fork;
+  ra.ev_join = c->ev_join;
   ZQ_CUDA(cudaEventRecord(c->ev_fork, st));
   ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
   if (int rc = refined_solve(ra)) return rc;

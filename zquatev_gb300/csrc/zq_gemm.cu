@@ -290,11 +290,13 @@ __global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDescT<R>* __re
   }
 }
 
-void k_dgemm_grouped_launch(const DgemmDesc* dev_descs, int count, int tiles, cudaStream_t st) {
+template <typename R>
+void grouped_launch(const DgemmDescT<R>* dev_descs, int count, int tiles, cudaStream_t st) {
   if (tiles <= 0 || count <= 0) return;
-  k_dgemm_grouped<double><<<tiles, GNT, 0, st>>>(dev_descs, count);
-  count_launch();
+  k_dgemm_grouped<R><<<tiles, GNT, 0, st>>>(dev_descs, count);
 }
+template void grouped_launch<double>(const DgemmDescT<double>*, int, int, cudaStream_t);
+template void grouped_launch<float>(const DgemmDescT<float>*, int, int, cudaStream_t);
 
 int dgemm_tiles(int m, int n) { return ceil_div(m, GT) * ceil_div(n, GT); }
 

@@ -72,7 +72,8 @@ struct DgemmDescT {
 using DgemmDesc = DgemmDescT<double>;
 template <typename R>
 int dgemm_grouped(DgemmDescT<R>* host_descs, int count, DgemmDescT<R>* dev_descs, cudaStream_t st);
-void k_dgemm_grouped_launch(const DgemmDesc* dev_descs, int count, int tiles, cudaStream_t st);
+template <typename R>
+void grouped_launch(const DgemmDescT<R>* dev_descs, int count, int tiles, cudaStream_t st);
 int dgemm_tiles(int m, int n);
 
 // ------------------------------------------------------------------ D&C (c)
@@ -101,6 +102,11 @@ struct DcPlan {
   DcWork w{};
   DcNode* nodes_dev = nullptr;
   DgemmDesc* descs_dev = nullptr;
+  // single-precision views of Z and M, and their descriptors (after the double
+  // ones and two spare slots in the descriptor area)
+  float* Zf[2] = {nullptr, nullptr};
+  float* Mbf = nullptr;
+  DgemmDescT<float>* fdescs_dev = nullptr;
 
   static size_t workspace_doubles(int n);
   int build(int n);
@@ -109,6 +115,13 @@ struct DcPlan {
   int upload(double* ws, DcNode* dnodes, DgemmDesc* ddescs, cudaStream_t st);
   // d (n), e (n-1) on device; lam_out (n) on device; z_out points into the workspace
   int run(const double* d, const double* e, double* lam_out, double*& z_out, cudaStream_t st);
+  // same tree with Z and the merge products in FP32 (eigenvalues and the
+  // secular equation stay FP64): the refined path's decomposition
+  int run_single(const double* d, const double* e, double* lam_out, float*& z_out, cudaStream_t st);
+  // descriptor area bytes for upload(): double descriptors + 2 spare + float descriptors
+  static size_t desc_bytes(size_t ndescs) {
+    return sizeof(DgemmDescT<double>) * (ndescs + 2) + sizeof(DgemmDescT<float>) * ndescs;
+  }
 };
 
 // ------------------------------------------------------------ back-transform
@@ -139,6 +152,8 @@ struct RefineArgs {
   double cluster_tol;          // accepted in-cluster coupling (relative to max |lambda|)
   double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap|
   cudaStream_t st;
+  cudaStream_t st2;            // second stream: Q formation overlaps the tridiagonal solve
+  cudaEvent_t ev_fork, ev_join;
   int iters; double last_emax;  // outputs
   double last_cluster;         // in-cluster coupling of the last step (before rotation)
   int clusters;                // clusters resolved (-1: one too large)

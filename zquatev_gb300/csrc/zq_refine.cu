@@ -54,19 +54,15 @@ __global__ void k_c64_to_c128(const float2* __restrict__ src, int64_t lds, doubl
     dst[r + (int64_t)c * ldd] = make_double2((double)v.x, (double)v.y);
   }
 }
-__global__ void k_d_to_f(const double* __restrict__ src, float* __restrict__ dst, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-    dst[t] = (float)src[t];
-}
-// x += (double) y   (2D, complex)
-__global__ void k_add_c64_to_c128(const float2* __restrict__ y, int64_t ldy, double2* __restrict__ x, int64_t ldx,
-                                  int rows, int cols) {
+// x += y   (2D, complex FP64)
+__global__ void k_add_c128(const double2* __restrict__ y, int64_t ldy, double2* __restrict__ x, int64_t ldx, int rows,
+                           int cols) {
   const int64_t total = (int64_t)rows * cols;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(t % rows), c = (int)(t / rows);
-    const float2 v = y[r + (int64_t)c * ldy];
+    const double2 v = y[r + (int64_t)c * ldy];
     double2 w = x[r + (int64_t)c * ldx];
-    w.x += (double)v.x; w.y += (double)v.y;
+    w.x += v.x; w.y += v.y;
     x[r + (int64_t)c * ldx] = w;
   }
 }
@@ -130,7 +126,7 @@ __global__ void k_oa_norms(const double2* __restrict__ S1, const double2* __rest
 __global__ void k_oa_build_e(const double2* __restrict__ S1, const double2* __restrict__ S2,
                              const double2* __restrict__ G1, const double2* __restrict__ G2, int64_t ld, int n,
                              const double* __restrict__ lam, const double* __restrict__ part, int nparts,
-                             float2* __restrict__ Et, float2* __restrict__ Eb, int64_t lde, double* __restrict__ emax,
+                             double2* __restrict__ Et, double2* __restrict__ Eb, int64_t lde, double* __restrict__ emax,
                              int* __restrict__ pair_count, int2* __restrict__ pairs, int pair_cap, double eps_pair) {
   __shared__ double sh[32];
   __shared__ double s_lm;
@@ -180,8 +176,8 @@ __global__ void k_oa_build_e(const double2* __restrict__ S1, const double2* __re
       const int q = atomicAdd(pair_count, 1);
       if (q < pair_cap) pairs[q] = make_int2(i, j);
     }
-    Et[i + (int64_t)j * lde] = make_float2((float)e1.x, (float)e1.y);
-    Eb[i + (int64_t)j * lde] = make_float2((float)e2.x, (float)e2.y);
+    Et[i + (int64_t)j * lde] = e1;
+    Eb[i + (int64_t)j * lde] = e2;
     em = fmax(em, fmax(fabs(e1.x), fabs(e1.y)));
     em = fmax(em, fmax(fabs(e2.x), fabs(e2.y)));
   }
@@ -406,9 +402,7 @@ size_t refine_workspace_bytes(int n, int nbq) {
   b += sizeof(double2) * 2 * nn * 2;    // P1, P2 (2n x n each)
   b += sizeof(double2) * 2 * nn;        // HX
   b += sizeof(double2) * 4 * nn;        // G1, G2, S1, S2
-  b += sizeof(float2) * 2 * nn;         // Et, Eb
-  b += sizeof(float2) * 2 * nn * 2;     // Xf, XEf (2n x n each)
-  b += sizeof(float) * nn;              // Zf
+  b += sizeof(double2) * 2 * nn;        // Et, Eb
   b += tridiag_workspace_bytes<float>(n, 64);
   b += form_q_workspace_bytes(n, nbq);  // sized for double2, enough for float2
   b += sizeof(double) * (45 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64);
@@ -560,11 +554,8 @@ int refined_solve(RefineArgs& ra) {
   double2* G2 = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
   double2* S1 = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
   double2* S2 = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
-  float2* Et = reinterpret_cast<float2*>(take(sizeof(float2) * nn));
-  float2* Eb = reinterpret_cast<float2*>(take(sizeof(float2) * nn));
-  float2* Xf = reinterpret_cast<float2*>(take(sizeof(float2) * 2 * nn));
-  float2* XEf = reinterpret_cast<float2*>(take(sizeof(float2) * 2 * nn));
-  float* Zf = reinterpret_cast<float*>(take(sizeof(float) * nn));
+  double2* Et = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
+  double2* Eb = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
   void* tri_ws = take(tridiag_workspace_bytes<float>(n, 64));
   void* fq_ws = take(form_q_workspace_bytes(n, ra.nbq));
   double* sm = reinterpret_cast<double*>(take(sizeof(double) * (45 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64)));
@@ -592,12 +583,15 @@ int refined_solve(RefineArgs& ra) {
   TridiagView<float> vf = tridiag_bind<float>(tri_ws, Mf, n, n2, 64, d, e, tau);
   if (int rc = tridiagonalize<float>(vf, ra.nb, st)) return rc;
   if (int rc = phase_reduce(e, n, offd, phi, st)) return rc;
-  double* Zd = nullptr;
-  if (int rc = ra.dc->run(d, offd, lam, Zd, st)) return rc;
   float2* XfQ = Mf + (int64_t)n * n2;  // right half of Mf
-  if (int rc = form_q<float>(Mf, n2, n, phi, XfQ, n2, ra.nbq, fq_ws, st)) return rc;
-  k_d_to_f<<<grid_for((int64_t)nn), 256, 0, st>>>(Zd, Zf, (int64_t)nn);
-  ZQ_LAUNCH_CHECK();
+  // Q Phi (FP32) on the second stream while the divide and conquer runs
+  ZQ_CUDA(cudaEventRecord(ra.ev_fork, st));
+  ZQ_CUDA(cudaStreamWaitEvent(ra.st2, ra.ev_fork, 0));
+  if (int rc = form_q<float>(Mf, n2, n, phi, XfQ, n2, ra.nbq, fq_ws, ra.st2)) return rc;
+  ZQ_CUDA(cudaEventRecord(ra.ev_join, ra.st2));
+  float* Zf = nullptr;  // FP32 divide and conquer: Z in the plan's workspace
+  if (int rc = ra.dc->run_single(d, offd, lam, Zf, st)) return rc;
+  ZQ_CUDA(cudaStreamWaitEvent(st, ra.ev_join, 0));
   if (int rc = apply_z<float>(XfQ, n2, Zf, n, n, Mf, n2, ra.fdesc, st)) return rc;
   k_c64_to_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(Mf, n2, X, ldd, n2, n);
   ZQ_LAUNCH_CHECK();
@@ -676,18 +670,17 @@ int refined_solve(RefineArgs& ra) {
     if (ra.clusters < 0) break;
     ra.last_emax = em;
     ra.last_cluster = cm;
-    // X += X E_top + J conj(X) E_bot  (FP32 product, FP64 accumulation)
-    k_c128_to_c64<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(X, ldd, Xf, n2, n2, n);
-    ZQ_LAUNCH_CHECK();
-    ZgemmArgsT<float> f{};
-    const float2 fone = make_float2(1.f, 0.f), fzero = make_float2(0.f, 0.f);
-    f.m = n; f.n = n; f.k1 = n; f.k2 = n;
-    f.A1 = Xf; f.lda1 = n2; f.B1 = Et; f.ldb1 = n; f.A2 = Xf + n; f.lda2 = n2; f.B2 = Eb; f.ldb2 = n; f.s2 = -1.f;
-    f.alpha = fone; f.beta = fzero; f.C = XEf; f.ldc = n2;
-    if (int rc = zgemm<float>(OP_N, OP_N, OP_R, OP_N, f, 1, st)) return rc;
-    f.A1 = Xf + n; f.A2 = Xf; f.s2 = 1.f; f.C = XEf + n;
-    if (int rc = zgemm<float>(OP_N, OP_N, OP_R, OP_N, f, 1, st)) return rc;
-    k_add_c64_to_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(XEf, n2, X, ldd, n2, n);
+    // X += X E_top + J conj(X) E_bot: the correction is small (|E| <= 1e-4), so
+    // a 4-slice (28-bit) Ozaki product is accurate enough; FP64 accumulation
+    //   P1_top = U E_top - conj(V) E_bot,  P1_bot = V E_top + conj(U) E_bot
+    g = ZgemmArgs{};
+    g.m = n; g.n = n; g.k1 = n; g.k2 = n;
+    g.A1 = U; g.lda1 = ldd; g.B1 = Et; g.ldb1 = n; g.A2 = V; g.lda2 = ldd; g.B2 = Eb; g.ldb2 = n; g.s2 = -1.0;
+    g.alpha = one; g.beta = zero; g.C = P1; g.ldc = n2;
+    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_R, OP_N, g, ra.ows, ra.ows_bytes, st, 4, 0, 0)) return rc;
+    g.A1 = V; g.A2 = U; g.s2 = 1.0; g.C = P1 + n;
+    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_R, OP_N, g, ra.ows, ra.ows_bytes, st, 4, 0, 0)) return rc;
+    k_add_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(P1, n2, X, ldd, n2, n);
     ZQ_LAUNCH_CHECK();
     ra.iters = it + 1;
     if (trace)

@@ -44,16 +44,18 @@ __device__ __forceinline__ int dc_find_node(const DcNode* nodes, int cnt, int po
   return -1;
 }
 
-__global__ void k_dc_leaf(const DcNode* nodes, int cnt, const double* dmod, double* Zout, double* lamout, int n) {
+template <typename ZT>
+__global__ void k_dc_leaf(const DcNode* nodes, int cnt, const double* dmod, ZT* Zout, double* lamout, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cnt) return;
   const int a = nodes[i].a;
-  Zout[a + (int64_t)a * n] = 1.0;
+  Zout[a + (int64_t)a * n] = (ZT)1;
   lamout[a] = dmod[a];
 }
 
 // one CTA per internal node
-__global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, const double* Zin, const double* lamin, int n) {
+template <typename ZT>
+__global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, const ZT* Zin, const double* lamin, int n) {
   DcNode& nd = nodes[blockIdx.x];
   const int a = nd.a, c = nd.c, b = nd.b;
   const int m = b - a, n1 = c - a, n2 = b - c;
@@ -66,7 +68,7 @@ __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, con
     int pos;
     if (i < n1) {
       val = lamin[a + i];
-      z = Zin[(c - 1) + (int64_t)(a + i) * n] * rs2;
+      z = (double)Zin[(c - 1) + (int64_t)(a + i) * n] * rs2;
       // count of right values strictly less than val
       int lo = 0, hi = n2;
       while (lo < hi) { const int mid = (lo + hi) >> 1; if (lamin[c + mid] < val) lo = mid + 1; else hi = mid; }
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, con
     } else {
       const int i2 = i - n1;
       val = lamin[c + i2];
-      z = Zin[c + (int64_t)(a + i) * n] * rs2;
+      z = (double)Zin[c + (int64_t)(a + i) * n] * rs2;
       int lo = 0, hi = n1;
       while (lo < hi) { const int mid = (lo + hi) >> 1; if (lamin[a + mid] <= val) lo = mid + 1; else hi = mid; }
       pos = i2 + lo;
@@ -243,7 +245,8 @@ __global__ void k_dc_zhat(const DcNode* nodes, int cnt, DcWork w) {
 }
 
 // one CTA per column slot of every internal node: writes a full column of M
-__global__ void __launch_bounds__(128) k_dc_vectors(const DcNode* nodes, int cnt, DcWork w, double* Mb, double* lamout, int n) {
+template <typename ZT>
+__global__ void __launch_bounds__(128) k_dc_vectors(const DcNode* nodes, int cnt, DcWork w, ZT* Mb, double* lamout, int n) {
   const int pos = blockIdx.x;
   const int ni = dc_find_node(nodes, cnt, pos);
   if (ni < 0) return;
@@ -266,8 +269,8 @@ __global__ void __launch_bounds__(128) k_dc_vectors(const DcNode* nodes, int cnt
     while (lo < hi) { const int mid = (lo + hi) >> 1; if (w.r_lam[a + mid] <= val) lo = mid + 1; else hi = mid; }
     outpos = i + lo;
   }
-  double* col = Mb + a + (int64_t)(a + outpos) * n;
-  for (int r = tid; r < m; r += blockDim.x) col[r] = 0.0;
+  ZT* col = Mb + a + (int64_t)(a + outpos) * n;
+  for (int r = tid; r < m; r += blockDim.x) col[r] = (ZT)0;
   __syncthreads();
   if (s < K) {
     const double* D = w.nd_val + a;
@@ -287,29 +290,30 @@ __global__ void __launch_bounds__(128) k_dc_vectors(const DcNode* nodes, int cnt
     const double inv = 1.0 / nrm;
     for (int k = tid; k < K; k += blockDim.x) {
       const double del = (D[k] - Do) - t;
-      col[w.nd_col[a + k]] = w.zhat[a + k] / del * inv;
+      col[w.nd_col[a + k]] = (ZT)(w.zhat[a + k] / del * inv);
     }
   } else {
-    if (tid == 0) col[w.df_scol[a + (s - K)]] = 1.0;
+    if (tid == 0) col[w.df_scol[a + (s - K)]] = (ZT)1;
   }
   if (tid == 0) lamout[a + outpos] = val;
 }
 
 // apply the deflation rotations (in reverse order) to every column of M
-__global__ void k_dc_rotate(const DcNode* nodes, int cnt, DcWork w, double* Mb, int n) {
+template <typename ZT>
+__global__ void k_dc_rotate(const DcNode* nodes, int cnt, DcWork w, ZT* Mb, int n) {
   const int pos = blockIdx.x * blockDim.x + threadIdx.x;
   const int ni = dc_find_node(nodes, cnt, pos);
   if (ni < 0) return;
   const DcNode nd = nodes[ni];
   if (nd.nrot == 0) return;
   const int a = nd.a;
-  double* col = Mb + a + (int64_t)pos * n;
+  ZT* col = Mb + a + (int64_t)pos * n;
   for (int r = nd.nrot - 1; r >= 0; --r) {
     const int P = w.rot_p[a + r], J = w.rot_j[a + r];
     const double c = w.rot_c[a + r], s = w.rot_s[a + r];
     const double vp = col[P], vj = col[J];
-    col[P] = c * vp - s * vj;
-    col[J] = s * vp + c * vj;
+    col[P] = (ZT)(c * vp - s * vj);
+    col[J] = (ZT)(s * vp + c * vj);
   }
 }
 
@@ -462,59 +466,100 @@ int DcPlan::upload(double* ws, DcNode* dnodes, DgemmDesc* ddescs, cudaStream_t s
       d.C = Z[t & 1] + d.off_c;
     }
   }
+  // single-precision views of the same buffers (Z, M as float) for run_single
+  Zf[0] = reinterpret_cast<float*>(Z[0]);
+  Zf[1] = reinterpret_cast<float*>(Z[1]);
+  Mbf = reinterpret_cast<float*>(Mb);
+  fdescs_dev = reinterpret_cast<DgemmDescT<float>*>(ddescs + gemm_host.size() + 2);
+  std::vector<DgemmDescT<float>> fbound(gemm_host.size());
+  for (size_t i = 0; i < gemm_host.size(); ++i) {
+    const DgemmDesc& h = gemm_host[i];
+    DgemmDescT<float>& f = fbound[i];
+    f.lda = h.lda; f.ldb = h.ldb; f.ldc = h.ldc;
+    f.off_a = h.off_a; f.off_b = h.off_b; f.off_c = h.off_c;
+    f.m = h.m; f.n = h.n; f.k = h.k; f.ta = h.ta; f.tb = h.tb; f.tile0 = h.tile0;
+    f.alpha = 1.f; f.beta = 0.f;
+  }
+  for (int t = 0; t <= max_depth; ++t) {
+    for (int q = 0; q < 2 * depth_cnt[t]; ++q) {
+      DgemmDescT<float>& d = fbound[gemm_off[t] + q];
+      d.A = Zf[(t + 1) & 1] + d.off_a;
+      d.B = Mbf + d.off_b;
+      d.C = Zf[t & 1] + d.off_c;
+    }
+  }
   if (!nodes_host.empty())
     ZQ_CUDA(cudaMemcpyAsync(dnodes, nodes_host.data(), sizeof(DcNode) * nodes_host.size(), cudaMemcpyHostToDevice, st));
   if (!bound.empty())
     ZQ_CUDA(cudaMemcpyAsync(ddescs, bound.data(), sizeof(DgemmDesc) * bound.size(), cudaMemcpyHostToDevice, st));
+  if (!fbound.empty())
+    ZQ_CUDA(cudaMemcpyAsync(fdescs_dev, fbound.data(), sizeof(DgemmDescT<float>) * fbound.size(), cudaMemcpyHostToDevice,
+                            st));
   // the host copies must outlive the async copies: synchronise once at plan time
   ZQ_CUDA(cudaStreamSynchronize(st));
   return ZQ_OK;
 }
 
-int DcPlan::run(const double* d, const double* e, double* lam_out, double*& z_out, cudaStream_t st) {
-  if (n <= 0) return ZQ_OK;
+template <typename ZT>
+static int dc_run(DcPlan& P, const double* d, const double* e, double* lam_out, ZT* const Zb[2], ZT* Mb,
+                  const DgemmDescT<ZT>* descs, cudaStream_t st) {
+  const int n = P.n;
   // scale, tear
-  k_dc_maxabs<<<1, 1024, 0, st>>>(d, e, n, scal);
+  k_dc_maxabs<<<1, 1024, 0, st>>>(d, e, n, P.scal);
   ZQ_LAUNCH_CHECK();
-  k_dc_scale_in<<<ceil_div(n, 256), 256, 0, st>>>(d, e, n, dmod, es, scal);
+  k_dc_scale_in<<<ceil_div(n, 256), 256, 0, st>>>(d, e, n, P.dmod, P.es, P.scal);
   ZQ_LAUNCH_CHECK();
-  if (!nodes_host.empty()) {
-    k_dc_setrho<<<ceil_div((int)nodes_host.size(), 256), 256, 0, st>>>(nodes_dev, (int)nodes_host.size(), es);
+  if (!P.nodes_host.empty()) {
+    k_dc_setrho<<<ceil_div((int)P.nodes_host.size(), 256), 256, 0, st>>>(P.nodes_dev, (int)P.nodes_host.size(), P.es);
     ZQ_LAUNCH_CHECK();
   }
   // Z buffers need zeros outside the diagonal blocks only where they are read:
   // every read is inside a node's block, which is fully written first.
-  for (int t = max_depth; t >= 0; --t) {
-    double* Zo = Z[t & 1];
-    double* Zi = Z[(t + 1) & 1];
-    double* lo = lam[t & 1];
-    const double* li = lam[(t + 1) & 1];
-    if (leaf_cnt[t] > 0) {
-      k_dc_leaf<<<ceil_div(leaf_cnt[t], 128), 128, 0, st>>>(nodes_dev + leaf_off[t], leaf_cnt[t], dmod, Zo, lo, n);
+  for (int t = P.max_depth; t >= 0; --t) {
+    ZT* Zo = Zb[t & 1];
+    ZT* Zi = Zb[(t + 1) & 1];
+    double* lo = P.lam[t & 1];
+    const double* li = P.lam[(t + 1) & 1];
+    if (P.leaf_cnt[t] > 0) {
+      k_dc_leaf<ZT><<<ceil_div(P.leaf_cnt[t], 128), 128, 0, st>>>(P.nodes_dev + P.leaf_off[t], P.leaf_cnt[t], P.dmod, Zo,
+                                                                    lo, n);
       ZQ_LAUNCH_CHECK();
     }
-    const int cnt = depth_cnt[t];
+    const int cnt = P.depth_cnt[t];
     if (cnt == 0) continue;
-    DcNode* nd = nodes_dev + depth_off[t];
-    k_dc_prepare<<<cnt, 256, 0, st>>>(nd, w, Zi, li, n);
+    DcNode* nd = P.nodes_dev + P.depth_off[t];
+    k_dc_prepare<ZT><<<cnt, 256, 0, st>>>(nd, P.w, Zi, li, n);
     ZQ_LAUNCH_CHECK();
-    k_dc_secular<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, w);
+    k_dc_secular<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, P.w);
     ZQ_LAUNCH_CHECK();
-    k_dc_zhat<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, w);
+    k_dc_zhat<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, P.w);
     ZQ_LAUNCH_CHECK();
-    k_dc_vectors<<<n, 128, 0, st>>>(nd, cnt, w, Mb, lo, n);
+    k_dc_vectors<ZT><<<n, 128, 0, st>>>(nd, cnt, P.w, Mb, lo, n);
     ZQ_LAUNCH_CHECK();
-    k_dc_rotate<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, w, Mb, n);
+    k_dc_rotate<ZT><<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, P.w, Mb, n);
     ZQ_LAUNCH_CHECK();
-    if (gemm_tiles[t] > 0) {
-      k_dgemm_grouped_launch(descs_dev + gemm_off[t], 2 * cnt, gemm_tiles[t], st);
+    if (P.gemm_tiles[t] > 0) {
+      grouped_launch<ZT>(descs + P.gemm_off[t], 2 * cnt, P.gemm_tiles[t], st);
       ZQ_LAUNCH_CHECK();
     }
   }
-  k_dc_unscale<<<ceil_div(n, 256), 256, 0, st>>>(lam[0], n, scal);
+  k_dc_unscale<<<ceil_div(n, 256), 256, 0, st>>>(P.lam[0], n, P.scal);
   ZQ_LAUNCH_CHECK();
-  ZQ_CUDA(cudaMemcpyAsync(lam_out, lam[0], sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  ZQ_CUDA(cudaMemcpyAsync(lam_out, P.lam[0], sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  return ZQ_OK;
+}
+
+int DcPlan::run(const double* d, const double* e, double* lam_out, double*& z_out, cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  if (int rc = dc_run<double>(*this, d, e, lam_out, Z, Mb, descs_dev, st)) return rc;
   z_out = Z[0];
+  return ZQ_OK;
+}
+
+int DcPlan::run_single(const double* d, const double* e, double* lam_out, float*& z_out, cudaStream_t st) {
+  if (n <= 0) return ZQ_OK;
+  if (int rc = dc_run<float>(*this, d, e, lam_out, Zf, Mbf, fdescs_dev, st)) return rc;
+  z_out = Zf[0];
   return ZQ_OK;
 }
 
