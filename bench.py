@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--serve-lanes", type=int, default=4)
     p.add_argument("--batch-count", type=int, default=4096, help="matrices in the batched run (0 skips it)")
     p.add_argument("--profile-path", default="default", choices=["default", "fp64", "batched"])
+    p.add_argument("--clustered-n2", type=int, default=0,
+                   help="also measure the clustered-spectrum workload (e.g. 16384): refined vs FP64, errors")
     p.add_argument("--profile-n2", type=int, default=0,
                    help="profiling case: run --reps device-resident solves of this size (--profile-path) and exit")
     p.add_argument("--reps", type=int, default=1)
@@ -401,6 +403,54 @@ def batched_case(count: int, fp64_peak: float, seed: int = 2024) -> dict:
             "max_residual_sampled": worst}
 
 
+# ------------------------------------------------------- clustered spectrum
+def clustered_case(n2: int) -> dict:
+    """One matrix H = Q diag(lam) Q^H (Q quaternion-unitary; 80% of lam uniform in
+    [-10, 10], 20% in clusters of 8 with gaps 1e-6), solved by the default
+    (refined) path and by the plain FP64 path; per-eigenvalue error against the
+    constructed spectrum, residual and orthonormality of both (GPU torch FP64 as
+    the checker)."""
+    import torch
+
+    from zquatev_gb300 import _lib, inputs, metrics, solver
+
+    lib = _lib.load()
+    n = n2 // 2
+    t0 = time.perf_counter()
+    master, lam = inputs.clustered_matrix_device(n, 2023)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    lam_sorted = torch.from_numpy(np.sort(lam)).cuda()
+    st = torch.cuda.current_stream().cuda_stream
+    out = {"workload": f"n2={n2} clustered: H = Q diag(lam) Q^H, 20% of lam in clusters of 8 (gap 1e-6)",
+           "generation_s": gen_s}
+    for name, fn in (("refined", lib.zquatev_device), ("fp64", lib.zquatev_fp64_device)):
+        work = master.clone()
+        deig = torch.zeros(n2, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = fn(n2, work.data_ptr(), n2, deig.data_ptr(), st)
+        e1.record()
+        torch.cuda.synchronize()
+        assert rc == 0, _lib.last_error()
+        r = {"ms": e0.elapsed_time(e1)}
+        if name == "refined":
+            it, corr, fb = solver.refine_stats()
+            r.update({"refine_iterations": it, "last_correction": corr, "fp64_fallback": fb})
+        r["eig_error"] = float((deig[:n] - lam_sorted).abs().max() / lam_sorted.abs().max())
+        h = master.T
+        v = work.T
+        r["residual"] = metrics.torch_residual(h, v, deig[:n])
+        r["orthonormality"] = metrics.torch_orthonormality(v)
+        out[name] = r
+        del work, v
+    out["speedup"] = out["fp64"]["ms"] / out["refined"]["ms"]
+    del master
+    torch.cuda.empty_cache()
+    return out
+
+
 # --------------------------------------------------------------- serving
 def serving_requests(count: int, seed: int = 4242):
     """Mixed stream: n log-uniform in [32, 2048]; 70% random (as config 0),
@@ -677,6 +727,7 @@ def main():
     del master, work
     torch.cuda.empty_cache()
     batched = batched_case(args.batch_count, fp64_peak) if (rank == 0 and args.batch_count > 0) else None
+    clustered = clustered_case(args.clustered_n2) if (rank == 0 and args.clustered_n2 > 0) else None
     serving = None
     if rank == 0 and args.serve_requests > 0:
         serving = serving_case(args.serve_requests, [float(x) for x in args.serve_rates.split(",")], args.serve_lanes)
@@ -736,6 +787,8 @@ def main():
             line["serving"] = serving
         if batched is not None:
             line["batched"] = batched
+        if clustered is not None:
+            line["clustered"] = clustered
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -115,9 +115,9 @@ def clustered_matrix_device(n: int, seed: int):
     """(D as a torch (n2, n2) complex128 CUDA tensor holding column-major D, lambda).
 
     Large-n version of clustered_matrix: the quaternion-unitary Q is the
-    eigenvector matrix (exactly (U -V*; V U*)-structured) that the FP64 GPU path
-    returns for a random quaternion-Hermitian matrix, and H = Q diag(lam, lam) Q^H
-    is formed with torch FP64 products on the GPU.
+    eigenvector matrix (exactly (U -V*; V U*)-structured, orthonormal to ~1e-14)
+    that the GPU drop-in returns for a random quaternion-Hermitian matrix, and
+    H = Q diag(lam, lam) Q^H is formed with torch FP64 products on the GPU.
     """
     import torch
 
@@ -128,9 +128,9 @@ def clustered_matrix_device(n: int, seed: int):
     d = random_matrix(n, seed + 104729)
     dq = torch.from_numpy(np.ascontiguousarray(d.T)).cuda()
     de = torch.zeros(n2, dtype=torch.float64, device="cuda")
-    rc = lib.zquatev_fp64_device(n2, dq.data_ptr(), n2, de.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    rc = lib.zquatev_device(n2, dq.data_ptr(), n2, de.data_ptr(), torch.cuda.current_stream().cuda_stream)
     if rc != 0:
-        raise RuntimeError(f"zquatev_fp64_device rc={rc}: {_lib.last_error()}")
+        raise RuntimeError(f"zquatev_device rc={rc}: {_lib.last_error()}")
     q = dq.T  # (n2, n2) column-major view: columns are eigenvectors
     lam = clustered_spectrum(n, seed)
     lt = torch.from_numpy(np.concatenate([lam, lam])).cuda().to(torch.complex128)
