@@ -56,6 +56,18 @@ template <typename Z> __host__ __device__ __forceinline__ void cfmacb(Z& acc, Z 
 
 template <typename Z> __host__ __device__ __forceinline__ Z czero() { Z z; z.x = 0; z.y = 0; return z; }
 
+// (I, J), I >= J, of lower-triangle tile t in row order (t = I (I + 1) / 2 + J).
+// FP32 square root for the estimate, exact integer correction (GB300's FP64
+// pipe is 1/64 of its FP32 rate, so no double arithmetic per thread here).
+__device__ __forceinline__ void tri_tile(int t, int& I, int& J) {
+  int i = (int)((__fsqrt_rn(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  if (i < 0) i = 0;
+  while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+  while ((long long)i * (i + 1) / 2 > t) --i;
+  I = i;
+  J = t - (int)((long long)i * (i + 1) / 2);
+}
+
 // ----------------------------------------------------------------------------
 // block reductions
 // ----------------------------------------------------------------------------

@@ -200,10 +200,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 3) k_oz_gemm(OzGemmArgs g) {
   int bi = blockIdx.x, bj = blockIdx.y;
   if (g.lower) {
     const int t = blockIdx.x;
-    int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while ((I + 1) * (I + 2) / 2 <= t) ++I;
-    while (I * (I + 1) / 2 > t) --I;
-    bi = I; bj = t - I * (I + 1) / 2;
+    tri_tile(t, bi, bj);
   }
   const int i0 = bi * OZ_TM, j0 = bj * OZ_TN;
   int sc = 0;

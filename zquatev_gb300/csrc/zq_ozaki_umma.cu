@@ -182,11 +182,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   int bi = blockIdx.x, bj = blockIdx.y;
   if (g.lower) {
     const int t = blockIdx.x;
-    int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while ((I + 1) * (I + 2) / 2 <= t) ++I;
-    while (I * (I + 1) / 2 > t) --I;
-    bi = I;
-    bj = t - I * (I + 1) / 2;
+    tri_tile(t, bi, bj);
   }
   const int i0 = bi * UM_BM, j0 = bj * UM_BN;
   const int Kp = g.Kp;

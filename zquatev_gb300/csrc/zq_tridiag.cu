@@ -32,11 +32,10 @@
 //   colupd  (finish y_{k-1}; apply the panel's deferred updates to column k;
 //            norm partials)
 //   reflect (build w in place of x; dot-product partials vs previous W, Y)
-//   dotsum  (reduce those partials)
 //   hemv    (quaternion Hermitian mat-vec of the panel-start trailing matrix,
 //            lower triangles of A and B only, per-tile deterministic partials)
-//   hreduce (sum tile partials, subtract the deferred-update corrections -> g;
-//            partials of c)
+//   hreduce (sum tile partials and the dot partials, subtract the
+//            deferred-update corrections -> g; partials of c)
 // All arithmetic is FP64 (template R = double) for the plain path; the same
 // kernels instantiate with R = float for the mixed-precision path, where norms
 // and reflector scalars are still formed in double.
@@ -268,25 +267,6 @@ __global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, 
 }
 
 // ----------------------------------------------------------------------------
-// dotsum: reduce dot partials -> dots[i*4 + q]
-// ----------------------------------------------------------------------------
-template <typename R>
-__global__ void k_dotsum(TridiagView<R> v, int k, int ndp) {
-  using Z = cplx<R>;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int t = warp; t < 4 * k; t += nw) {
-    const int i = t >> 2, q = t & 3;
-    R sx = 0, sy = 0;
-    for (int c = lane; c < ndp; c += 32) {
-      const Z p = v.dpart[((int64_t)c * v.nbmax + i) * 4 + q];
-      sx += p.x; sy += p.y;
-    }
-    sx = warp_sum(sx); sy = warp_sum(sy);
-    if (lane == 0) v.dots[t] = mk(sx, sy);
-  }
-}
-
-// ----------------------------------------------------------------------------
 // hemv: quaternion Hermitian mat-vec of the panel-start trailing matrix.
 //   Region rows/cols [r0, n); lower-triangle 32x32 tiles, one CTA per tile.
 //   The A and B tiles are staged in shared memory (padded, conflict-free for
@@ -310,10 +290,8 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
   const Z* B = v.M + n;
   const int r0 = j + 1;
   const int t = blockIdx.x;
-  int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while ((I + 1) * (I + 2) / 2 <= t) ++I;
-  while (I * (I + 1) / 2 > t) --I;
-  const int J = t - I * (I + 1) / 2;
+  int I, J;
+  tri_tile(t, I, J);
   const bool diag = (I == J);
   const int tid = threadIdx.x;
   const int rbase = r0 + I * HT, cbase = r0 + J * HT;
@@ -387,9 +365,16 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
 // ----------------------------------------------------------------------------
 // hreduce: g = H_panelstart w - corrections, for rows [j+1, n); c partials.
 //   T is the hemv tile edge used for this column; nblk its number of blocks.
+//   HRB rows per CTA; four threads per (row, product) sum the hemv tile
+//   partials (fixed split and combine order: deterministic). Every CTA also
+//   sums the reflect kernel's dot partials (ndp of them) itself, in the same
+//   fixed order, so no separate reduction launch sits between reflect and hemv.
 // ----------------------------------------------------------------------------
+constexpr int HRB = 16;          // rows per CTA
+constexpr int HNG = NT / HRB;    // reflector groups for the corrections
 template <typename R>
-__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode) {
+__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode,
+                                                int ndp) {
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -397,38 +382,60 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
   const Z* B = v.M + n;
   const int r0 = j + 1;
   const int tid = threadIdx.x;
-  const int row = tid & (RB - 1), grp = tid >> 5;
-  const int lrow = blockIdx.x * RB + row;   // row index inside the region
+  const int row = tid & (HRB - 1), grp = tid >> 4;
+  const int lrow = blockIdx.x * HRB + row;   // row index inside the region
   const int r = r0 + lrow;
-  __shared__ Z s_v[RB][4];
+  __shared__ Z s_v[HRB][4];
   __shared__ Z s_dots[4 * 64];
-  __shared__ Z s_red[NG][RB][2];
+  __shared__ Z s_part[4][4 * HRB];
+  __shared__ Z s_dsub[NT];
+  __shared__ Z s_red[HNG][HRB][2];
   __shared__ double s_redd[NT / 32];
-  __shared__ Z s_half[4 * RB];
   if (!zero_mode) {
-    const int o = tid & (4 * RB - 1), half = tid >> 7;   // 128 outputs x 2 halves
+    // (1) tile partials: output o = (row, product), quarter q sums blocks S = q, q + 4, ...
+    const int o = tid & (4 * HRB - 1), quarter = tid >> 6;
     const int orow = o >> 2, ou = o & 3;
-    const int lr = blockIdx.x * RB + orow;
+    const int lr = blockIdx.x * HRB + orow;
     Z s0 = czero<Z>(), s1 = czero<Z>();
     if (r0 + lr < n) {
       const int Rb = lr / T, off = lr % T;
       const int nbm = v.hblk;
       const Z* base = v.hpart + (((int64_t)Rb * nbm) * T + off) * 4 + ou;
       const int64_t stride = (int64_t)T * 4;
-      int S = half;
-      for (; S + 2 < nblk; S += 4) { s0 = cadd(s0, base[S * stride]); s1 = cadd(s1, base[(S + 2) * stride]); }
-      for (; S < nblk; S += 2) s0 = cadd(s0, base[S * stride]);
+      int S = quarter;
+      for (; S + 4 < nblk; S += 8) { s0 = cadd(s0, base[S * stride]); s1 = cadd(s1, base[(S + 4) * stride]); }
+      for (; S < nblk; S += 4) s0 = cadd(s0, base[S * stride]);
     }
-    if (half == 1) s_half[o] = cadd(s0, s1);
-    __syncthreads();
-    if (half == 0) s_v[orow][ou] = cadd(cadd(s0, s1), s_half[o]);
+    s_part[quarter][o] = cadd(s0, s1);
+    // (2) dot products of the panel: 4k outputs, the ndp partials split over NT / 4k threads each
+    if (k > 0) {
+      const int no = 4 * k;
+      const int nsub = NT / no;
+      const int t = tid % no, sub = tid / no;
+      Z acc = czero<Z>();
+      if (sub < nsub) {
+        const int i = t >> 2, q = t & 3;
+        for (int c = sub; c < ndp; c += nsub) acc = cadd(acc, v.dpart[((int64_t)c * v.nbmax + i) * 4 + q]);
+      }
+      s_dsub[tid] = acc;
+    }
   }
-  for (int t = tid; t < 4 * k; t += NT) s_dots[t] = v.dots[t];
+  __syncthreads();
+  if (!zero_mode) {
+    if (tid < 4 * HRB)
+      s_v[tid >> 2][tid & 3] = cadd(cadd(s_part[0][tid], s_part[1][tid]), cadd(s_part[2][tid], s_part[3][tid]));
+    if (k > 0 && tid < 4 * k) {
+      const int no = 4 * k, nsub = NT / no;
+      Z d = s_dsub[tid];
+      for (int sub = 1; sub < nsub; ++sub) d = cadd(d, s_dsub[sub * no + tid]);
+      s_dots[tid] = d;
+    }
+  }
   __syncthreads();
   // deferred-update corrections, reflectors split over the groups
   Z ta = czero<Z>(), tb = czero<Z>();
   if (!zero_mode && r < n) {
-    for (int i = grp; i < k; i += NG) {
+    for (int i = grp; i < k; i += HNG) {
       const Z s1 = s_dots[4 * i + 0], s2 = s_dots[4 * i + 1], s3 = s_dots[4 * i + 2], s4 = s_dots[4 * i + 3];
       const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
       const Z ya = v.Ya[r + (int64_t)i * v.ldy], yb = v.Yb[r + (int64_t)i * v.ldy];
@@ -448,7 +455,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
       // ha = A x - conj(B z), hb = B x + conj(A z)
       ga = csub(s_v[row][0], cconj(s_v[row][3]));
       gb = cadd(s_v[row][2], cconj(s_v[row][1]));
-      for (int g2 = 0; g2 < NG; ++g2) { ga = csub(ga, s_red[g2][row][0]); gb = csub(gb, s_red[g2][row][1]); }
+      for (int g2 = 0; g2 < HNG; ++g2) { ga = csub(ga, s_red[g2][row][0]); gb = csub(gb, s_red[g2][row][1]); }
       const Z wa = A[r + (int64_t)j * ld], wb = B[r + (int64_t)j * ld];
       cp = (double)(wa.x * ga.x + wa.y * ga.y + wb.x * gb.x + wb.y * gb.y);
     }
@@ -472,10 +479,8 @@ __global__ void __launch_bounds__(NT) k_trail(TridiagView<R> v, int p, int nbp, 
   Z* A = v.M;
   Z* B = v.M + n;
   const int t = blockIdx.x;
-  int I = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while ((I + 1) * (I + 2) / 2 <= t) ++I;
-  while (I * (I + 1) / 2 > t) --I;
-  const int J = t - I * (I + 1) / 2;
+  int I, J;
+  tri_tile(t, I, J);
   const int tid = threadIdx.x;
   const int tr = tid & 15, tc = tid >> 4;
   const int rb = t0 + I * TB, cb = t0 + J * TB;
@@ -576,10 +581,6 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
       ZQ_LAUNCH_CHECK();
       const int T = HT;
       const int nblk = ceil_div(L, T);
-      if (L >= 2 && k > 0) {
-        k_dotsum<R><<<1, NT, 0, st>>>(v, k, ncta2);
-        ZQ_LAUNCH_CHECK();
-      }
       prof_end(PC_PANEL, st);
       if (L >= 2) {
         prof_begin(PC_HEMV, st);
@@ -588,8 +589,8 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
         prof_end(PC_HEMV, st);
       }
       prof_begin(PC_PANEL, st);
-      const int nhr = ceil_div(L, RB);
-      k_hreduce<R><<<nhr, NT, 0, st>>>(v, p, j, k, T, nblk, L < 2 ? 1 : 0);
+      const int nhr = ceil_div(L, HRB);
+      k_hreduce<R><<<nhr, NT, 0, st>>>(v, p, j, k, T, nblk, L < 2 ? 1 : 0, ncta2);
       ZQ_LAUNCH_CHECK();
       prof_end(PC_PANEL, st);
       ncp = nhr;
@@ -622,7 +623,7 @@ size_t tridiag_workspace_bytes(int n, int nbmax) {
   b += sizeof(Z) * ((hblk + 2) * (hblk + 2) * 32 * 4);  // hpart: 32-tiles, or 64-tiles at the same block stride
   b += sizeof(Z) * (hblk * nbmax * 4);                // dpart
   b += sizeof(Z) * (4 * (size_t)nbmax);               // dots
-  b += sizeof(double) * (3 * hblk + 8);               // npart, cpart, scal
+  b += sizeof(double) * (4 * hblk + 8);               // npart (2 hblk), cpart (one per 16 rows), scal
   return b + 16 * 256;
 }
 
@@ -642,7 +643,7 @@ TridiagView<R> tridiag_bind(void* ws, cplx<R>* M, int n, int64_t ld, int nbmax, 
   v.dpart = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)hblk * nbmax * 4));
   v.dots = reinterpret_cast<Z*>(take(sizeof(Z) * 4 * (size_t)nbmax));
   v.npart = reinterpret_cast<double*>(take(sizeof(double) * 2 * hblk));
-  v.cpart = reinterpret_cast<double*>(take(sizeof(double) * hblk));
+  v.cpart = reinterpret_cast<double*>(take(sizeof(double) * 2 * hblk));
   v.scal = reinterpret_cast<double*>(take(sizeof(double) * 8));
   v.d = d; v.e = e; v.tau = tau;
   return v;
