@@ -68,6 +68,12 @@ __device__ __forceinline__ void tri_tile(int t, int& I, int& J) {
   J = t - (int)((long long)i * (i + 1) / 2);
 }
 
+// Programmatic dependent launch: a kernel launched with launch_pdl may begin
+// while the previous kernel on the stream drains; it must execute pdl_wait()
+// (griddepcontrol.wait: returns once the preceding grid has completed and its
+// memory is visible) before touching anything that grid produced.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ----------------------------------------------------------------------------
 // block reductions
 // ----------------------------------------------------------------------------
@@ -140,6 +146,21 @@ enum Status : int {
   } while (0)
 
 void count_launch(int k = 1);
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 void set_last_error(cudaError_t e, const char* what, const char* file, int line);
 void set_error_message(const char* msg);

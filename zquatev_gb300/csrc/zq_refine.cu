@@ -607,8 +607,13 @@ int refined_solve(RefineArgs& ra) {
   const bool trace = getenv("ZQ_REFINE_TRACE") != nullptr;  // per-step history on stderr
   for (int it = 0; it < ra.max_iter; ++it) {
     // the first correction only has to reach ~1e-8 (the next step squares the
-    // error): 5 slices (35 bits); later steps use 8 (56 bits)
+    // error): 5 slices (35 bits); later steps use 8 (56 bits: 7 slices would
+    // save a fifth of the products but cost ~25x in eigenvalue accuracy)
     const int sl = (it == 0) ? 5 : 8;
+    // the correction X E is small (|E| <= 1e-4 in the first step, ~1e-8 after):
+    // 3 slices (21 bits) first, 4 (28 bits) after keep its error below what
+    // the next step removes / below 1e-14
+    const int sl_upd = (it == 0) ? 3 : 4;
     double2* U = X;
     double2* V = X + n;
     ZgemmArgs g{};
@@ -670,16 +675,15 @@ int refined_solve(RefineArgs& ra) {
     if (ra.clusters < 0) break;
     ra.last_emax = em;
     ra.last_cluster = cm;
-    // X += X E_top + J conj(X) E_bot: the correction is small (|E| <= 1e-4), so
-    // a 4-slice (28-bit) Ozaki product is accurate enough; FP64 accumulation
+    // X += X E_top + J conj(X) E_bot with sl_upd slices; FP64 accumulation
     //   P1_top = U E_top - conj(V) E_bot,  P1_bot = V E_top + conj(U) E_bot
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n; g.k2 = n;
     g.A1 = U; g.lda1 = ldd; g.B1 = Et; g.ldb1 = n; g.A2 = V; g.lda2 = ldd; g.B2 = Eb; g.ldb2 = n; g.s2 = -1.0;
     g.alpha = one; g.beta = zero; g.C = P1; g.ldc = n2;
-    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_R, OP_N, g, ra.ows, ra.ows_bytes, st, 4, 0, 0)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_R, OP_N, g, ra.ows, ra.ows_bytes, st, sl_upd, 0, 0)) return rc;
     g.A1 = V; g.A2 = U; g.s2 = 1.0; g.C = P1 + n;
-    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_R, OP_N, g, ra.ows, ra.ows_bytes, st, 4, 0, 0)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_R, OP_N, g, ra.ows, ra.ows_bytes, st, sl_upd, 0, 0)) return rc;
     k_add_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(P1, n2, X, ldd, n2, n);
     ZQ_LAUNCH_CHECK();
     ra.iters = it + 1;

@@ -36,6 +36,8 @@
 //            lower triangles of A and B only, per-tile deterministic partials)
 //   hreduce (sum tile partials and the dot partials, subtract the
 //            deferred-update corrections -> g; partials of c)
+// The kernels are launched with programmatic dependent launch (each starts
+// with pdl_wait), so a kernel's launch overlaps the tail of the previous one.
 // All arithmetic is FP64 (template R = double) for the plain path; the same
 // kernels instantiate with R = float for the mixed-precision path, where norms
 // and reflector scalars are still formed in double.
@@ -54,6 +56,7 @@ constexpr int NT = 256;       // threads per CTA
 // ----------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, int k, int ncp, int do_update) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -163,6 +166,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
 // ----------------------------------------------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, int k, int nnp) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -283,6 +287,7 @@ constexpr int HT = 32;        // hemv tile edge
 constexpr int HLD = HT + 1;   // padded shared leading dimension
 template <typename R>
 __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -375,6 +380,7 @@ constexpr int HNG = NT / HRB;    // reflector groups for the corrections
 template <typename R>
 __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode,
                                                 int ndp) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -473,6 +479,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
 constexpr int KC = 4;  // reflectors per smem stage
 template <typename R>
 __global__ void __launch_bounds__(NT) k_trail(TridiagView<R> v, int p, int nbp, int t0) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -573,25 +580,25 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
       const int L = n - 1 - j;
       const int ncta1 = ceil_div(n - j, RB);
       prof_begin(PC_PANEL, st);
-      k_colupd<R><<<ncta1, NT, 0, st>>>(v, p, j, k, ncp, 1);
-      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(launch_pdl(k_colupd<R>, dim3(ncta1), dim3(NT), st, v, p, j, k, ncp, 1));
+      count_launch();
       if (L < 1) { prof_end(PC_PANEL, st); ncp = 0; continue; }
       const int ncta2 = ceil_div(L, RB);
-      k_reflect<R><<<ncta2, NT, 0, st>>>(v, p, j, k, ncta1);
-      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(launch_pdl(k_reflect<R>, dim3(ncta2), dim3(NT), st, v, p, j, k, ncta1));
+      count_launch();
       const int T = HT;
       const int nblk = ceil_div(L, T);
       prof_end(PC_PANEL, st);
       if (L >= 2) {
         prof_begin(PC_HEMV, st);
-        k_hemv<R><<<nblk * (nblk + 1) / 2, 128, 0, st>>>(v, j);
-        ZQ_LAUNCH_CHECK();
+        ZQ_CUDA(launch_pdl(k_hemv<R>, dim3(nblk * (nblk + 1) / 2), dim3(128), st, v, j));
+        count_launch();
         prof_end(PC_HEMV, st);
       }
       prof_begin(PC_PANEL, st);
       const int nhr = ceil_div(L, HRB);
-      k_hreduce<R><<<nhr, NT, 0, st>>>(v, p, j, k, T, nblk, L < 2 ? 1 : 0, ncta2);
-      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(launch_pdl(k_hreduce<R>, dim3(nhr), dim3(NT), st, v, p, j, k, T, nblk, L < 2 ? 1 : 0, ncta2));
+      count_launch();
       prof_end(PC_PANEL, st);
       ncp = nhr;
     }
@@ -599,13 +606,13 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
     if (t0 < n) {
       // finish y of the panel's last reflector (rows >= t0), then update
       prof_begin(PC_PANEL, st);
-      k_colupd<R><<<ceil_div(n - t0, RB), NT, 0, st>>>(v, p, t0, nbp, ncp, 0);
-      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(launch_pdl(k_colupd<R>, dim3(ceil_div(n - t0, RB)), dim3(NT), st, v, p, t0, nbp, ncp, 0));
+      count_launch();
       prof_end(PC_PANEL, st);
       const int nblk = ceil_div(n - t0, TB);
       prof_begin(PC_TRAIL, st);
-      k_trail<R><<<nblk * (nblk + 1) / 2, NT, 0, st>>>(v, p, nbp, t0);
-      ZQ_LAUNCH_CHECK();
+      ZQ_CUDA(launch_pdl(k_trail<R>, dim3(nblk * (nblk + 1) / 2), dim3(NT), st, v, p, nbp, t0));
+      count_launch();
       prof_end(PC_TRAIL, st);
       ncp = 0;
     }
