@@ -139,9 +139,12 @@ __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, con
   }
 }
 
-// secular equation: one thread per root
-__global__ void k_dc_secular(const DcNode* nodes, int cnt, DcWork w) {
-  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+// secular equation: one warp per root; the lanes split the sums over the
+// poles (butterfly reductions leave identical totals on every lane, so the
+// iteration's control flow stays warp-uniform)
+__global__ void __launch_bounds__(128) k_dc_secular(const DcNode* nodes, int cnt, DcWork w) {
+  const int pos = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   const int ni = dc_find_node(nodes, cnt, pos);
   if (ni < 0) return;
   const DcNode nd = nodes[ni];
@@ -156,8 +159,9 @@ __global__ void k_dc_secular(const DcNode* nodes, int cnt, DcWork w) {
   if (i < K - 1) {
     const double gap = D[i + 1] - D[i];
     const double mid = 0.5 * gap;
-    double f = 1.0;
-    for (int k = 0; k < K; ++k) f += rho * z[k] * z[k] / ((D[k] - D[i]) - mid);
+    double fs = 0.0;
+    for (int k = lane; k < K; k += 32) fs += rho * z[k] * z[k] / ((D[k] - D[i]) - mid);
+    const double f = 1.0 + warp_sum(fs);
     if (f >= 0.0) { o = i; lo = 0.0; hi = mid; }
     else { o = i + 1; lo = -mid; hi = 0.0; }
   } else {
@@ -167,12 +171,13 @@ __global__ void k_dc_secular(const DcNode* nodes, int cnt, DcWork w) {
   double tau = 0.5 * (lo + hi);
   for (int it = 0; it < 200; ++it) {
     double psi = 0.0, phi = 0.0, dpsi = 0.0, dphi = 0.0;
-    for (int k = 0; k < K; ++k) {
+    for (int k = lane; k < K; k += 32) {
       const double del = (D[k] - Do) - tau;
       const double inv = 1.0 / del;
       const double t = rho * z[k] * z[k] * inv;
       if (k <= i) { psi += t; dpsi += t * inv; } else { phi += t; dphi += t * inv; }
     }
+    psi = warp_sum(psi); phi = warp_sum(phi); dpsi = warp_sum(dpsi); dphi = warp_sum(dphi);
     const double f = 1.0 + psi + phi;
     if (f == 0.0) break;
     if (f < 0.0) lo = tau; else hi = tau;
@@ -214,14 +219,18 @@ __global__ void k_dc_secular(const DcNode* nodes, int cnt, DcWork w) {
     if (tn == tau) break;
     tau = tn;
   }
-  w.r_orig[a + i] = o;
-  w.r_tau[a + i] = tau;
-  w.r_lam[a + i] = Do + tau;
+  if (lane == 0) {
+    w.r_orig[a + i] = o;
+    w.r_tau[a + i] = tau;
+    w.r_lam[a + i] = Do + tau;
+  }
 }
 
-// Gu-Eisenstat: zhat_k from the computed roots
-__global__ void k_dc_zhat(const DcNode* nodes, int cnt, DcWork w) {
-  const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+// Gu-Eisenstat: zhat_k from the computed roots; one warp per k, the product
+// over the roots split over the lanes
+__global__ void __launch_bounds__(128) k_dc_zhat(const DcNode* nodes, int cnt, DcWork w) {
+  const int pos = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   const int ni = dc_find_node(nodes, cnt, pos);
   if (ni < 0) return;
   const DcNode nd = nodes[ni];
@@ -233,15 +242,19 @@ __global__ void k_dc_zhat(const DcNode* nodes, int cnt, DcWork w) {
   const int* O = w.r_orig + a;
   const double* T = w.r_tau + a;
   // (lambda_{K-1} - D_k) / rho
-  double prod = ((D[O[K - 1]] - Dk) + T[K - 1]) / nd.rho2;
-  for (int j = 0; j < K - 1; ++j) {
+  double prod = (lane == 0) ? ((D[O[K - 1]] - Dk) + T[K - 1]) / nd.rho2 : 1.0;
+  for (int j = lane; j < K - 1; j += 32) {
     const double num = (D[O[j]] - Dk) + T[j];  // lambda_j - D_k
     const double den = (j < k) ? (D[j] - Dk) : (D[j + 1] - Dk);
     prod *= num / den;
   }
-  const double zk = w.nd_z[a + k];
-  const double zh = sqrt(fmax(prod, 0.0));
-  w.zhat[a + k] = (zk >= 0.0) ? zh : -zh;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) prod *= __shfl_xor_sync(0xffffffffu, prod, off);
+  if (lane == 0) {
+    const double zk = w.nd_z[a + k];
+    const double zh = sqrt(fmax(prod, 0.0));
+    w.zhat[a + k] = (zk >= 0.0) ? zh : -zh;
+  }
 }
 
 // one CTA per column slot of every internal node: writes a full column of M
@@ -530,9 +543,9 @@ static int dc_run(DcPlan& P, const double* d, const double* e, double* lam_out, 
     DcNode* nd = P.nodes_dev + P.depth_off[t];
     k_dc_prepare<ZT><<<cnt, 256, 0, st>>>(nd, P.w, Zi, li, n);
     ZQ_LAUNCH_CHECK();
-    k_dc_secular<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, P.w);
+    k_dc_secular<<<ceil_div(n, 4), 128, 0, st>>>(nd, cnt, P.w);
     ZQ_LAUNCH_CHECK();
-    k_dc_zhat<<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, P.w);
+    k_dc_zhat<<<ceil_div(n, 4), 128, 0, st>>>(nd, cnt, P.w);
     ZQ_LAUNCH_CHECK();
     k_dc_vectors<ZT><<<n, 128, 0, st>>>(nd, cnt, P.w, Mb, lo, n);
     ZQ_LAUNCH_CHECK();
