@@ -24,34 +24,77 @@
 
 namespace zq {
 
-// single thread: sequential quaternion products (n scalar steps)
-__global__ void k_phase(const double* e, int n, double* offd, double* phi) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double a0 = 1.0, a1 = 0.0, b0 = 0.0, b1 = 0.0;  // phi_0 = 1
-  phi[0] = a0; phi[1] = a1; phi[2] = b0; phi[3] = b1;
-  for (int k = 0; k + 1 < n; ++k) {
-    const double ea0 = e[4 * k], ea1 = e[4 * k + 1], eb0 = e[4 * k + 2], eb1 = e[4 * k + 3];
-    const double nrm = sqrt(ea0 * ea0 + ea1 * ea1 + eb0 * eb0 + eb1 * eb1);
+// Quaternion phases: phi_0 = 1, phi_{k+1} = u_k phi_k with u_k = e_k / |e_k|
+// (phi reset to 1 where e_k = 0), i.e. a segmented prefix product of unit
+// quaternions. One CTA: each thread takes a contiguous chunk, a Hillis-Steele
+// scan over the 1024 chunk products combines them (quaternion products are
+// associative), then every thread rewrites its chunk; each phi is normalised
+// when written.
+struct Quat { double a0, a1, b0, b1; int reset; };
+// q(a1, b1) q(a2, b2) = q(a1 a2 - conj(b1) b2, b1 a2 + conj(a1) b2)
+__device__ __forceinline__ Quat qmul(const Quat& x, const Quat& y) {
+  Quat r;
+  r.a0 = (x.a0 * y.a0 - x.a1 * y.a1) - (x.b0 * y.b0 + x.b1 * y.b1);
+  r.a1 = (x.a0 * y.a1 + x.a1 * y.a0) - (x.b0 * y.b1 - x.b1 * y.b0);
+  r.b0 = (x.b0 * y.a0 - x.b1 * y.a1) + (x.a0 * y.b0 + x.a1 * y.b1);
+  r.b1 = (x.b0 * y.a1 + x.b1 * y.a0) + (x.a0 * y.b1 - x.a1 * y.b0);
+  r.reset = 0;
+  return r;
+}
+// later o earlier (segmented: a reset in `later` drops `earlier`)
+__device__ __forceinline__ Quat qcombine(const Quat& later, const Quat& earlier) {
+  if (later.reset) return later;
+  Quat r = qmul(later, earlier);
+  r.reset = earlier.reset;
+  return r;
+}
+__device__ __forceinline__ Quat qunit_of(const double* e, int k, double& nrm) {
+  const double ea0 = e[4 * k], ea1 = e[4 * k + 1], eb0 = e[4 * k + 2], eb1 = e[4 * k + 3];
+  nrm = sqrt(ea0 * ea0 + ea1 * ea1 + eb0 * eb0 + eb1 * eb1);
+  Quat u;
+  if (nrm > 0.0) { const double s = 1.0 / nrm; u.a0 = ea0 * s; u.a1 = ea1 * s; u.b0 = eb0 * s; u.b1 = eb1 * s; u.reset = 0; }
+  else { u.a0 = 1.0; u.a1 = 0.0; u.b0 = 0.0; u.b1 = 0.0; u.reset = 1; }
+  return u;
+}
+constexpr int PH_T = 1024;
+__global__ void __launch_bounds__(PH_T) k_phase(const double* e, int n, double* offd, double* phi) {
+  __shared__ Quat s_q[PH_T];
+  const int t = threadIdx.x;
+  const int m = n - 1;                      // number of u_k
+  const int per = (m + PH_T - 1) / PH_T;
+  const int k0 = t * per, k1 = (k0 + per < m) ? k0 + per : m;
+  Quat acc{1.0, 0.0, 0.0, 0.0, 0};
+  for (int k = k0; k < k1; ++k) {
+    double nrm;
+    const Quat u = qunit_of(e, k, nrm);
+    acc = qcombine(u, acc);
+  }
+  s_q[t] = acc;
+  __syncthreads();
+  for (int off = 1; off < PH_T; off <<= 1) {
+    Quat v = s_q[t];
+    if (t >= off) v = qcombine(v, s_q[t - off]);
+    __syncthreads();
+    s_q[t] = v;
+    __syncthreads();
+  }
+  // exclusive prefix of this chunk = inclusive prefix of the previous one
+  Quat run = (t > 0) ? s_q[t - 1] : Quat{1.0, 0.0, 0.0, 0.0, 0};
+  if (t == 0) { phi[0] = 1.0; phi[1] = 0.0; phi[2] = 0.0; phi[3] = 0.0; }
+  for (int k = k0; k < k1; ++k) {
+    double nrm;
+    const Quat u = qunit_of(e, k, nrm);
     offd[k] = nrm;
-    if (nrm > 0.0) {
-      // q(ea, eb) * q(alpha, beta) = q(ea alpha - conj(eb) beta, eb alpha + conj(ea) beta)
-      double na0 = (ea0 * a0 - ea1 * a1) - (eb0 * b0 + eb1 * b1);
-      double na1 = (ea0 * a1 + ea1 * a0) - (eb0 * b1 - eb1 * b0);
-      double nb0 = (eb0 * a0 - eb1 * a1) + (ea0 * b0 + ea1 * b1);
-      double nb1 = (eb0 * a1 + eb1 * a0) + (ea0 * b1 - ea1 * b0);
-      const double s = 1.0 / sqrt(na0 * na0 + na1 * na1 + nb0 * nb0 + nb1 * nb1);
-      a0 = na0 * s; a1 = na1 * s; b0 = nb0 * s; b1 = nb1 * s;
-    } else {
-      a0 = 1.0; a1 = 0.0; b0 = 0.0; b1 = 0.0;
-    }
-    phi[4 * (k + 1) + 0] = a0; phi[4 * (k + 1) + 1] = a1;
-    phi[4 * (k + 1) + 2] = b0; phi[4 * (k + 1) + 3] = b1;
+    run = qcombine(u, run);
+    const double s = 1.0 / sqrt(run.a0 * run.a0 + run.a1 * run.a1 + run.b0 * run.b0 + run.b1 * run.b1);
+    phi[4 * (k + 1) + 0] = run.a0 * s; phi[4 * (k + 1) + 1] = run.a1 * s;
+    phi[4 * (k + 1) + 2] = run.b0 * s; phi[4 * (k + 1) + 3] = run.b1 * s;
   }
 }
 
 int phase_reduce(const double* e, int n, double* offd, double* phi, cudaStream_t st) {
   if (n <= 0) return ZQ_OK;
-  k_phase<<<1, 32, 0, st>>>(e, n, offd, phi);
+  k_phase<<<1, PH_T, 0, st>>>(e, n, offd, phi);
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;
 }

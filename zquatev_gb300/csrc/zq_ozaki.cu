@@ -106,6 +106,22 @@ __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict
   }
 }
 
+// base-128 digits of floor(|v| / 2^e * 2^(7 S)) (integer arithmetic on the
+// 53-bit significand: exact truncation), most significant first, and the sign
+__device__ __forceinline__ unsigned long long oz_fixed(double v, int e, int F, bool& neg) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  neg = (bits >> 63) != 0;
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  unsigned long long mant = bits & ((1ull << 52) - 1);
+  int ebits = ex;
+  if (ex == 0) ebits = 1; else mant |= (1ull << 52);
+  // |v| = mant * 2^(ebits - 1075);  V = floor(|v| 2^(F - e))
+  const int sh = ebits - 1075 - e + F;
+  if (mant == 0 || e < -1000) return 0;
+  if (sh >= 0) return (sh >= 64) ? 0 : (mant << sh);
+  return (-sh >= 64) ? 0 : (mant >> (-sh));
+}
+
 // S slices of one operand: out[t][idx][kp] (bf16), idx < padded count (zero rows above count).
 // The slices are the base-128 digits of floor(|v| / 2^e * 2^(7 S)) (integer
 // arithmetic on the 53-bit significand), with the sign of v: exact truncation.
@@ -122,28 +138,78 @@ __global__ void k_oz_slice(OzSide s, bool is_a, int count, int count_pad, int Kp
       oz_entry(s, is_a, idx, kp, v[0], v[1]);
       e = exps[idx];
     }
-    unsigned long long V[2];
     bool neg[2];
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
-      const unsigned long long bits = (unsigned long long)__double_as_longlong(v[c]);
-      neg[c] = (bits >> 63) != 0;
-      const int ex = (int)((bits >> 52) & 0x7ff);
-      unsigned long long mant = bits & ((1ull << 52) - 1);
-      int ebits = ex;
-      if (ex == 0) ebits = 1; else mant |= (1ull << 52);
-      // |v| = mant * 2^(ebits - 1075);  V = floor(|v| 2^(F - e))
-      const int sh = ebits - 1075 - e + F;
-      if (mant == 0 || e < -1000) V[c] = 0;
-      else if (sh >= 0) V[c] = (sh >= 64) ? 0 : (mant << sh);
-      else V[c] = (-sh >= 64) ? 0 : (mant >> (-sh));
-    }
+    const unsigned long long V0 = oz_fixed(v[0], e, F, neg[0]);
+    const unsigned long long V1 = oz_fixed(v[1], e, F, neg[1]);
     for (int q = 0; q < nsl; ++q) {
       const int shift = F - OZ_BETA * (q + 1);
-      const int dr = (int)((V[0] >> shift) & 127), di = (int)((V[1] >> shift) & 127);
+      const int dr = (int)((V0 >> shift) & 127), di = (int)((V1 >> shift) & 127);
       out_re[q * slice_stride + t] = __int2bfloat16_rn(neg[0] ? -dr : dr);
       if (out_im) out_im[q * slice_stride + t] = __int2bfloat16_rn(neg[1] ? -di : di);
     }
+  }
+}
+
+// Column-major A operands (op N or R: a row of op(A) is strided in memory):
+// the exponent pass and the slicing read 32 consecutive rows per warp.
+__global__ void k_oz_exp_init(int* __restrict__ exps, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) exps[i] = -1100;
+}
+// block (32, 8): 32 rows x 256 K terms; the per-row maximum exponent via atomicMax (order-free)
+__global__ void k_oz_exp_cm(OzSide s, int count, int Kp, int* __restrict__ exps) {
+  __shared__ int s_e[8][32];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int row = blockIdx.x * 32 + tx;
+  const int kb = blockIdx.y * 256;
+  int e = -1100;
+  if (row < count) {
+    for (int q = ty; q < 256; q += 8) {
+      const int kp = kb + q;
+      if (kp >= Kp) break;
+      double a, b;
+      oz_entry(s, true, row, kp, a, b);
+      if (a != 0.0) {
+        int ex;
+        frexp(a, &ex);  // 2^ex > |a|
+        e = ex > e ? ex : e;
+      }
+    }
+  }
+  s_e[ty][tx] = e;
+  __syncthreads();
+  if (ty == 0 && row < count) {
+    int m = s_e[0][tx];
+    for (int r = 1; r < 8; ++r) m = s_e[r][tx] > m ? s_e[r][tx] : m;
+    if (m > -1100) atomicMax(exps + row, m);
+  }
+}
+// block (32, 8): a 32-row x 32-K tile, digits staged in shared memory, stored along K
+__global__ void k_oz_slice_cm(OzSide s, int count, int Kp, const int* __restrict__ exps, int nsl,
+                              __nv_bfloat16* __restrict__ out, int64_t slice_stride) {
+  __shared__ __nv_bfloat16 s_d[OZ_SMAX][32][33];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int F = OZ_BETA * nsl;
+  const int row = i0 + tx;
+  const int e = row < count ? exps[row] : 0;
+  for (int kk = ty; kk < 32; kk += 8) {
+    const int kp = k0 + kk;
+    double v = 0.0, dummy;
+    if (row < count && kp < Kp) oz_entry(s, true, row, kp, v, dummy);
+    bool neg;
+    const unsigned long long V = oz_fixed(v, e, F, neg);
+    for (int q = 0; q < nsl; ++q) {
+      const int d = (int)((V >> (F - OZ_BETA * (q + 1))) & 127);
+      s_d[q][kk][tx] = __int2bfloat16_rn(neg ? -d : d);
+    }
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int kp = k0 + tx;
+    if (kp >= Kp) continue;
+    const int64_t o = (int64_t)(i0 + r) * Kp + kp;
+    for (int q = 0; q < nsl; ++q) out[q * slice_stride + o] = s_d[q][tx][r];
   }
 }
 
@@ -412,10 +478,23 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
   int* errf = reinterpret_cast<int*>(take(sizeof(int) * 4));
   auto grid = [](int64_t total) { int64_t x = (total + 255) / 256; return (int)(x > 16384 ? 16384 : x); };
   if (!opt.reuse_a) {
-    k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
-    ZQ_LAUNCH_CHECK();
-    k_oz_slice<<<grid(mp * Kp), 256, 0, st>>>(a, true, m, (int)mp, (int)Kp, ea, nsl, As, nullptr, mp * Kp);
-    ZQ_LAUNCH_CHECK();
+    const bool cm = (opa1 == OP_N || opa1 == OP_R) && (!two || opa2 == OP_N || opa2 == OP_R);
+    if (cm) {
+      // rows of op(A) are strided: column-wise passes (coalesced reads)
+      k_oz_exp_init<<<ceil_div(m, 256), 256, 0, st>>>(ea, m);
+      ZQ_LAUNCH_CHECK();
+      k_oz_exp_cm<<<dim3((unsigned)ceil_div(m, 32), (unsigned)ceil_div((int)Kp, 256)), dim3(32, 8), 0, st>>>(a, m, (int)Kp,
+                                                                                                             ea);
+      ZQ_LAUNCH_CHECK();
+      k_oz_slice_cm<<<dim3((unsigned)(mp / 32), (unsigned)ceil_div((int)Kp, 32)), dim3(32, 8), 0, st>>>(a, m, (int)Kp, ea,
+                                                                                                        nsl, As, mp * Kp);
+      ZQ_LAUNCH_CHECK();
+    } else {
+      k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
+      ZQ_LAUNCH_CHECK();
+      k_oz_slice<<<grid(mp * Kp), 256, 0, st>>>(a, true, m, (int)mp, (int)Kp, ea, nsl, As, nullptr, mp * Kp);
+      ZQ_LAUNCH_CHECK();
+    }
   }
   k_oz_exp<<<ceil_div(n * 32, 256), 256, 0, st>>>(b, false, n, (int)Kp, eb);
   ZQ_LAUNCH_CHECK();

@@ -617,17 +617,8 @@ int refined_solve(RefineArgs& ra) {
     double2* U = X;
     double2* V = X + n;
     ZgemmArgs g{};
-    // G1 = X^H X
-    g = ZgemmArgs{};
-    g.m = n; g.n = n; g.k1 = n2; g.A1 = X; g.lda1 = ldd; g.B1 = X; g.ldb1 = ldd;
-    g.alpha = one; g.beta = zero; g.C = G1; g.ldc = n;
-    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 0)) return rc;
-    // G2 = U^T V - V^T U
-    g = ZgemmArgs{};
-    g.m = n; g.n = n; g.k1 = n; g.k2 = n;
-    g.A1 = U; g.lda1 = ldd; g.B1 = V; g.ldb1 = ldd; g.A2 = V; g.lda2 = ldd; g.B2 = U; g.ldb2 = ldd; g.s2 = -1.0;
-    g.alpha = one; g.beta = zero; g.C = G2; g.ldc = n;
-    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 0)) return rc;
+    // Consecutive products share their A operand, so the second one reuses its
+    // slices: (P1, P2) with [A;B], (G1, S1) with X^H, (G2, S2) with [U^T | V^T].
     // P1 = [A;B] U, P2 = [A;B] conj(V)
     g = ZgemmArgs{};
     g.m = n2; g.n = n; g.k1 = n; g.A1 = H0; g.lda1 = n2; g.B1 = U; g.ldb1 = ldd;
@@ -637,16 +628,21 @@ int refined_solve(RefineArgs& ra) {
     if (int rc = zgemm_acc(ra.mode, OP_N, OP_R, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 0, 1)) return rc;
     k_hx_combine<<<grid_for((int64_t)nn), 256, 0, st>>>(P1, P2, n2, n, HX, n2);
     ZQ_LAUNCH_CHECK();
-    // S1 = X^H HX ; S2 = U^T HX_bot - V^T HX_top
+    // G1 = X^H X ; S1 = X^H HX
     g = ZgemmArgs{};
-    g.m = n; g.n = n; g.k1 = n2; g.A1 = X; g.lda1 = ldd; g.B1 = HX; g.ldb1 = n2;
-    g.alpha = one; g.beta = zero; g.C = S1; g.ldc = n;
+    g.m = n; g.n = n; g.k1 = n2; g.A1 = X; g.lda1 = ldd; g.B1 = X; g.ldb1 = ldd;
+    g.alpha = one; g.beta = zero; g.C = G1; g.ldc = n;
     if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 0)) return rc;
+    g.B1 = HX; g.ldb1 = n2; g.C = S1;
+    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 1)) return rc;
+    // G2 = U^T V - V^T U ; S2 = U^T HX_bot - V^T HX_top
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n; g.k2 = n;
-    g.A1 = U; g.lda1 = ldd; g.B1 = HX + n; g.ldb1 = n2; g.A2 = V; g.lda2 = ldd; g.B2 = HX; g.ldb2 = n2; g.s2 = -1.0;
-    g.alpha = one; g.beta = zero; g.C = S2; g.ldc = n;
+    g.A1 = U; g.lda1 = ldd; g.B1 = V; g.ldb1 = ldd; g.A2 = V; g.lda2 = ldd; g.B2 = U; g.ldb2 = ldd; g.s2 = -1.0;
+    g.alpha = one; g.beta = zero; g.C = G2; g.ldc = n;
     if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 0)) return rc;
+    g.B1 = HX + n; g.ldb1 = n2; g.B2 = HX; g.ldb2 = n2; g.C = S2;
+    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 1)) return rc;
     // Rayleigh quotients, coupling norms, E; pairs that fail the first-order
     // test are grouped into clusters, rotated (Rayleigh-Ritz on the current
     // basis, S and G carried along), and E is rebuilt in the rotated basis
