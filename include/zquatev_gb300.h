@@ -75,7 +75,7 @@ int zq_refine_stats(int* iters, double* last_correction, int* fell_back);
 /* Explicit paths of the host drop-in: plain FP64, or refined (with the FP64
  * fallback). zquatev_c / ts::zquatev / zquatev_device follow the path policy
  * set by zq_set_path: 0 FP64, 1 refined, 2 auto (default: refined for
- * n2 >= 512, FP64 below); environment ZQ_PATH=fp64|refined|auto overrides. */
+ * n2 >= 96, FP64 below); environment ZQ_PATH=fp64|refined|auto overrides. */
 int zquatev_fp64_c(int n2, double* D, int ld2, double* eig);
 int zquatev_refined_c(int n2, double* D, int ld2, double* eig);
 int zquatev_fp64_device(int n2, double* dD, int ld2, double* deig, void* stream);

@@ -204,7 +204,7 @@ def test_larger_random(gpu):
 @pytest.mark.parametrize("n", [40, 256, 700])
 def test_default_policy_drop_in(gpu, n):
     """The drop-in call (zquatev_c, the path ts::zquatev takes) meets the same bar
-    whichever path its policy picks (FP64 below n2 = 512, refined above)."""
+    whichever path its policy picks (FP64 below n2 = 96, refined from there)."""
     d = inputs.random_matrix(n, 8800 + n)
     out, eig = run(d, fn=solver.zquatev)
     check_solution(d, out, eig, n)

@@ -84,7 +84,7 @@ def test_routing_and_timestamps(gpu, batch_max_n2):
         assert info == 0
         if 2 * n <= batch_max_n2:
             assert t["path"] == "batched"
-        elif n >= 256:
+        elif n >= 48:
             assert t["path"] in ("refined", "refined->fp64")
         else:
             assert t["path"] == "fp64"

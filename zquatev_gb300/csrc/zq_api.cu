@@ -438,7 +438,7 @@ int path_for(int n) {
   if (const char* s = getenv("ZQ_PATH")) {
     if (!strcmp(s, "fp64")) p = 0; else if (!strcmp(s, "refined")) p = 1; else if (!strcmp(s, "auto")) p = 2;
   }
-  if (p == 2) p = (n >= 256) ? 1 : 0;
+  if (p == 2) p = (n >= 48) ? 1 : 0;  // refined measured faster from n = 48 up (2-4x)
   return p;
 }
 

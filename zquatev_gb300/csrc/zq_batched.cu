@@ -137,20 +137,27 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
     for (int i = tid; i < L; i += BT) {
       double2 ax = make_double2(0, 0), az = ax, bx = ax, bz = ax;
       const int gi = r0 + i;
-      for (int c = 0; c < L; ++c) {
-        const int gc = r0 + c;
+      // the three ranges of c (row i left of the diagonal, the diagonal, column
+      // i below it) in separate loops so the loads pipeline
+#pragma unroll 4
+      for (int c = 0; c < i; ++c) {
         const double2 x = swa[c], z = cconj(swb[c]);
-        if (c < i) {
-          const double2 am = A[gi + (int64_t)gc * ld], bm = B[gi + (int64_t)gc * ld];
-          cfma(ax, am, x); cfma(az, am, z); cfma(bx, bm, x); cfma(bz, bm, z);
-        } else if (c == i) {
-          const double am = A[gi + (int64_t)gi * ld].x;
-          ax.x += am * x.x; ax.y += am * x.y; az.x += am * z.x; az.y += am * z.y;
-        } else {
-          const double2 am = A[gc + (int64_t)gi * ld], bm = B[gc + (int64_t)gi * ld];
-          cfmac(ax, am, x); cfmac(az, am, z);           // conj(A[c,i])
-          cfma(bx, cneg(bm), x); cfma(bz, cneg(bm), z); // B[i,c] = -B[c,i]
-        }
+        const int64_t o = gi + (int64_t)(r0 + c) * ld;
+        const double2 am = A[o], bm = B[o];
+        cfma(ax, am, x); cfma(az, am, z); cfma(bx, bm, x); cfma(bz, bm, z);
+      }
+      {
+        const double2 x = swa[i], z = cconj(swb[i]);
+        const double am = A[gi + (int64_t)gi * ld].x;
+        ax.x += am * x.x; ax.y += am * x.y; az.x += am * z.x; az.y += am * z.y;
+      }
+#pragma unroll 4
+      for (int c = i + 1; c < L; ++c) {
+        const double2 x = swa[c], z = cconj(swb[c]);
+        const int64_t o = (r0 + c) + (int64_t)gi * ld;
+        const double2 am = A[o], bm = B[o];
+        cfmac(ax, am, x); cfmac(az, am, z);           // conj(A[c,i])
+        cfma(bx, cneg(bm), x); cfma(bz, cneg(bm), z); // B[i,c] = -B[c,i]
       }
       // ga = A x - conj(B z), gb = B x + conj(A z)
       const double2 ga = csub(ax, cconj(bz)), gb = cadd(bx, cconj(az));
@@ -163,20 +170,28 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
       syb[i] = csub(syb[i], cscale(swb[i], 0.5 * c));
     }
     __syncthreads();
-    // rank-2 structured update of the trailing lower triangles
-    for (int cc = 0; cc < L; ++cc) {
-      const double2 wac = swa[cc], wbc = swb[cc], yac = sya[cc], ybc = syb[cc];
-      const int gc = r0 + cc;
-      for (int i = cc + tid; i < L; i += BT) {
-        const double2 wai = swa[i], wbi = swb[i], yai = sya[i], ybi = syb[i];
+    // rank-2 structured update of the trailing lower triangles: each thread
+    // walks its row's segment (independent elements, so the loads pipeline)
+    for (int i = tid; i < L; i += BT) {
+      const double2 wai = swa[i], wbi = swb[i], yai = sya[i], ybi = syb[i];
+      const int64_t orow = r0 + i;
+#pragma unroll 4
+      for (int cc = 0; cc < i; ++cc) {
+        const double2 wac = swa[cc], wbc = swb[cc], yac = sya[cc], ybc = syb[cc];
+        const int64_t o = orow + (int64_t)(r0 + cc) * ld;
         double2 ta = make_double2(0, 0), tb = ta;
         cfmacb(ta, wai, yac); cfmac(ta, wbi, ybc); cfmacb(ta, yai, wac); cfmac(ta, ybi, wbc);
-        const int64_t o = (r0 + i) + (int64_t)gc * ld;
+        cfmacb(tb, wbi, yac); cfmac(tb, cneg(wai), ybc); cfmacb(tb, ybi, wac); cfmac(tb, cneg(yai), wbc);
+        const double2 av = A[o], bv = B[o];
+        A[o] = csub(av, ta);
+        B[o] = csub(bv, tb);
+      }
+      {  // diagonal element: A only (B's diagonal is zero)
+        const double2 wac = swa[i], wbc = swb[i], yac = sya[i], ybc = syb[i];
+        const int64_t o = orow + (int64_t)(r0 + i) * ld;
+        double2 ta = make_double2(0, 0);
+        cfmacb(ta, wai, yac); cfmac(ta, wbi, ybc); cfmacb(ta, yai, wac); cfmac(ta, ybi, wbc);
         A[o] = csub(A[o], ta);
-        if (i > cc) {
-          cfmacb(tb, wbi, yac); cfmac(tb, cneg(wai), ybc); cfmacb(tb, ybi, wac); cfmac(tb, cneg(yai), wbc);
-          B[o] = csub(B[o], tb);
-        }
       }
     }
     __syncthreads();
@@ -253,15 +268,20 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
       if (s_done) break;
       // apply the sweep's rotations (columns m-1 .. lo of Z) to every row
       const int m = s_m, cnt = s_cnt;
+      // the updated column i of one rotation is column i + 1 of the next: carry
+      // it in a register (no reload of a value just stored)
       for (int r = tid; r < n; r += BT) {
         double* zr = Z + r;
+        if (cnt == 0) continue;
+        double carry = zr[(int64_t)m * n];
         for (int q = 0; q < cnt; ++q) {
           const int i = m - 1 - q;
           const double c = sc_[q], s = ss_[q];
-          const double zi = zr[(int64_t)i * n], zi1 = zr[(int64_t)(i + 1) * n];
-          zr[(int64_t)(i + 1) * n] = s * zi + c * zi1;
-          zr[(int64_t)i * n] = c * zi - s * zi1;
+          const double zi = zr[(int64_t)i * n];
+          zr[(int64_t)(i + 1) * n] = s * zi + c * carry;
+          carry = c * zi - s * carry;
         }
+        zr[(int64_t)(m - cnt) * n] = carry;
       }
       __syncthreads();
     }
@@ -330,7 +350,7 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(BT) k_batched(BatchArgs a) {
+__global__ void __launch_bounds__(BT, 3) k_batched(BatchArgs a) {
   __shared__ int s_task;
   double* ws = a.ws + (int64_t)blockIdx.x * a.ws_stride;
   for (;;) {
