@@ -170,6 +170,14 @@ static int get_context(Context** out) {
     Context* c = nullptr;
     if (int rc = context_create(dev, &c)) return rc;
     g_ctx[dev] = c;
+    // the host entry points allocate the device copy of D per call from the
+    // stream-ordered pool: keep freed blocks mapped instead of returning them
+    // to the driver at every synchronisation
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
   }
   *out = g_ctx[dev];
   return ZQ_OK;
