@@ -151,6 +151,7 @@ struct RefineArgs {
   double tol;
   double cluster_tol;          // accepted in-cluster coupling (relative to max |lambda|)
   double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap|
+  int slices0;                 // Ozaki slices of the first step's products
   cudaStream_t st;
   cudaStream_t st2;            // second stream: Q formation overlaps the tridiagonal solve
   cudaEvent_t ev_fork, ev_join;

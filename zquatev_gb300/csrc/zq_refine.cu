@@ -607,9 +607,10 @@ int refined_solve(RefineArgs& ra) {
   const bool trace = getenv("ZQ_REFINE_TRACE") != nullptr;  // per-step history on stderr
   for (int it = 0; it < ra.max_iter; ++it) {
     // the first correction only has to reach ~1e-8 (the next step squares the
-    // error): 5 slices (35 bits); later steps use 8 (56 bits: 7 slices would
-    // save a fifth of the products but cost ~25x in eigenvalue accuracy)
-    const int sl = (it == 0) ? 5 : 8;
+    // error): ZQ_REFINE_SLICES0 slices (default 5 = 35 bits); later steps use 8
+    // (56 bits: 7 slices would save a fifth of the products but cost ~25x in
+    // eigenvalue accuracy)
+    const int sl = (it == 0) ? ra.slices0 : 8;
     // the correction X E is small (|E| <= 1e-4 in the first step, ~1e-8 after):
     // 3 slices (21 bits) first, 4 (28 bits) after keep its error below what
     // the next step removes / below 1e-14
