@@ -71,6 +71,17 @@ def parse():
     return p.parse_args()
 
 
+def max_over_ranks(value: float, world: int, device) -> float:
+    """The slowest rank's time (all ranks receive it); value itself for one rank."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -664,11 +675,7 @@ def main():
     barrier()
     launches = lib.zq_launch_count() - launches0
     lib.zq_profile_enable(0)
-    ms_total = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(e0.elapsed_time(e1), world, dev)
     ms_step = ms_total / args.steps
     prof = {k: _lib.profile_read(k) for k in ("ozaki", "refine", "tridiag", "stedc", "formq", "apply_z")}
     oz_flops = _lib.profile_flops("ozaki") / args.steps

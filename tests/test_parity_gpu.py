@@ -282,3 +282,21 @@ def test_batched_equals_single(gpu):
         assert metrics.eig_error(eig[:n], seig[:n], hn) <= TOL
         assert metrics.subspace_distance(out, eig[:n], sout, seig[:n], 1e-6 * hn) < 1e-8
         assert metrics.residual(h, out, eig[:n]) <= TOL
+
+
+@pytest.mark.parametrize("fn", [solver.zquatev_fp64, solver.zquatev_refined], ids=["fp64", "refined"])
+def test_block_diagonal_input(gpu, fn):
+    """Two independent quaternion blocks: the reduction meets an exactly zero
+    column below the first block (zero off-diagonal quaternion), where the
+    phase chain restarts."""
+    n1, n2b = 30, 50
+    a1, b1 = inputs.random_blocks(n1, 71)
+    a2, b2 = inputs.random_blocks(n2b, 72)
+    n = n1 + n2b
+    a = np.zeros((n, n), dtype=np.complex128)
+    b = np.zeros((n, n), dtype=np.complex128)
+    a[:n1, :n1], a[n1:, n1:] = a1, a2
+    b[:n1, :n1], b[n1:, n1:] = b1, b2
+    d = inputs.pack_left_half(a, b)
+    out, eig = run(d, fn=fn)
+    check_solution(d, out, eig, n)
