@@ -177,7 +177,7 @@ void prof_begin(int cls, cudaStream_t st);
 void prof_end(int cls, cudaStream_t st);
 void prof_add_flops(int cls, double flops);
 
-inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
-inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 }  // namespace zq
