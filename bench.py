@@ -71,6 +71,14 @@ def parse():
     return p.parse_args()
 
 
+def workload_config(n2: int, world: int) -> dict:
+    """The measured workload, identical on the GPU arm and the reference arm."""
+    return {"workload": f"single quaternion-Hermitian solve n2={n2} (n={n2 // 2}): random A=(X+X^H)/2, "
+                        "B=(Y-Y^T)/2 (Re, Im ~ N(0,1)), complex128, all eigenvalues and eigenvectors",
+            "n2": n2, "parallelism": f"replicas{world}",
+            "l2": "inputs (512 MiB left half) larger than L2; restored D2D each step"}
+
+
 def max_over_ranks(value: float, world: int, device) -> float:
     """The slowest rank's time (all ranks receive it); value itself for one rank."""
     if world <= 1:
@@ -284,8 +292,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": f"single quaternion-Hermitian solve n2={args.n2} (random, complex128), "
-                               f"timed as n2={args.cpu_sample_n2} samples scaled by n^3"},
+        "config": workload_config(args.n2, world),
         "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": "port",
                          "sample": f"one n2={args.cpu_sample_n2} solve per step through oracle/port.py "
                                    f"(numpy + scipy OpenBLAS/LAPACK), x{(args.n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
@@ -765,10 +772,9 @@ def main():
             "vs_baseline": None,
             "dtype": "f64 (FP32 decomposition + bf16-Ozaki-refined to FP64 accuracy)",
             "data": "synthetic",
-            "config": {"workload": f"single quaternion-Hermitian solve n2={n2} (n={n}), random A=(X+X^H)/2, "
-                                   "B=(Y-Y^T)/2, complex128, all eigenvectors, drop-in default path (refined)",
-                       "n2": n2, "nb_tuned": tuned_nb, "parallelism": f"replicas{world}",
-                       "l2": "inputs (512 MiB left half) larger than L2; restored D2D each step"},
+            "config": workload_config(n2, world),
+            "path": "drop-in default: FP32 decomposition + Ozaki-product refinement to FP64 accuracy",
+            "nb_tuned": tuned_nb,
             "fp64_path_ms": fp64_ms,
             "speedup_vs_fp64_path": fp64_ms / ms_step if ms_step > 0 else None,
             "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": n2 * n * 16,
