@@ -11,8 +11,8 @@ flush is needed between steps.
 
   value   device-resident: the input is restored from an HBM master copy
           (device-to-device) and solved through the device C ABI; ms per solve.
-  e2e     the reference-facing host call (zquatev_c on a host array): H2D of
-          the left half, solve, D2H of all of D and eig, per solve.
+  e2e     the reference-facing host call (zquatev_c on pinned host arrays): H2D
+          of the left half, solve, D2H of all of D and eig, per solve.
   roofline  the dominant kernel (the Ozaki tensor-core product), timed with
           CUDA events on its launch stream during the timed region, executed
           bf16 flops against MEASURED_PEAKS.json's sustained bf16 figure; the
@@ -717,12 +717,15 @@ def main():
     lib.zq_profile_enable(0)
     fprof = {k: _lib.profile_read(k) for k in ("hemv", "trail", "formq_gemm", "apply_z", "stedc", "tridiag", "formq")}
 
-    # end to end through the host C ABI (H2D + solve + D2H inside)
-    # (one untimed call first: it maps the device copy of D in the stream-ordered pool)
+    # end to end through the host C ABI (H2D + solve + D2H inside), from and to
+    # pinned host arrays (one untimed call first: it maps the device copy of D
+    # in the stream-ordered pool)
+    pinned_d = torch.empty((n2, n2), dtype=torch.complex128, pin_memory=True)
+    dh = pinned_d.numpy().T  # column-major (Fortran) view, ld2 = n2
+    eh = torch.zeros(n2, dtype=torch.float64, pin_memory=True).numpy()
     e2e_ms = []
     for i in range(args.e2e_steps + 1):
-        dh = d_host.copy(order="F")
-        eh = np.zeros(n2)
+        dh[...] = d_host
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rc = solver.zquatev(n2, dh, n2, eh)
@@ -778,7 +781,8 @@ def main():
             "fp64_path_ms": fp64_ms,
             "speedup_vs_fp64_path": fp64_ms / ms_step if ms_step > 0 else None,
             "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": n2 * n * 16,
-                    "d2h_bytes_per_step": n2 * n2 * 16 + n * 8},
+                    "d2h_bytes_per_step": n2 * n2 * 16 + n * 8, "host_memory": "pinned",
+                    "samples_ms": [round(x, 1) for x in e2e_ms]},
             "gpu_launches": None,
             "roofline": {"bound": "tensor", "kernel": "k_oz_umma (bf16 tcgen05.mma, TMEM accumulators, TMA; Ozaki slices)",
                          "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",

@@ -300,3 +300,32 @@ def test_block_diagonal_input(gpu, fn):
     d = inputs.pack_left_half(a, b)
     out, eig = run(d, fn=fn)
     check_solution(d, out, eig, n)
+
+
+@pytest.mark.parametrize("memory", ["pageable", "pageable-unregistered", "pinned"])
+def test_host_memory_kinds(gpu, memory, monkeypatch):
+    """The host drop-in on pageable arrays (page-locked for the call, or copied
+    as they are with ZQ_HOST_REGISTER=0) and on pinned arrays: same result,
+    padding rows of a larger ld2 untouched. D is 31 MB, above the 8 MB
+    registration threshold."""
+    import torch
+
+    n = 700
+    n2, ld2 = 2 * n, 2 * n + 6
+    d0 = inputs.random_matrix(n, 77)
+    if memory == "pinned":
+        buf = torch.empty((n2, ld2), dtype=torch.complex128, pin_memory=True)
+        d = buf.numpy().T
+        d[...] = inputs.random_matrix(n, 77, ld2=ld2)
+        eig = torch.full((n2,), 7.25, dtype=torch.float64, pin_memory=True).numpy()
+    else:
+        d = np.asfortranarray(inputs.random_matrix(n, 77, ld2=ld2))
+        eig = np.full(n2, 7.25)
+    if memory == "pageable-unregistered":
+        monkeypatch.setenv("ZQ_HOST_REGISTER", "0")
+    d[n2:, :] = 123.0
+    rc = solver.zquatev(n2, d, ld2, eig)
+    assert rc == 0, (rc, _lib.last_error())
+    assert np.all(d[n2:, :] == 123.0)
+    assert np.all(eig[n:] == 7.25)
+    check_solution(d0, np.asarray(d[:n2]), eig, n)
