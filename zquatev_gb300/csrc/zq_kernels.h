@@ -27,7 +27,8 @@ struct TridiagView {
   cplx<R>* dots;   // 4 * nbmax
   double* npart;   // norm partials: 2 * hblk
   double* cpart;   // c partials: hblk
-  double* scal;    // per-column scalars (8)
+  double* scal;    // per-column scalars (16): [0..3] x_1 of the column, [4] f, [5..8] f m (reflector head)
+  unsigned* counter;  // colupd CTAs finished for the current column (the last one forms the reflector)
   double* d;       // diagonal (n)
   double* e;       // quaternion subdiagonal (4 doubles each, n)
   double* tau;     // 1 if reflector j exists else 0 (n)

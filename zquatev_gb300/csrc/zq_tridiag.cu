@@ -30,12 +30,15 @@
 //
 // Per column the launch sequence is
 //   colupd  (finish y_{k-1}; apply the panel's deferred updates to column k;
-//            norm partials)
-//   reflect (build w in place of x; dot-product partials vs previous W, Y)
-//   hemv    (quaternion Hermitian mat-vec of the panel-start trailing matrix,
-//            lower triangles of A and B only, per-tile deterministic partials)
+//            norm partials; the last CTA to finish combines them into the
+//            reflector head f, f m and the subdiagonal entry e_j)
+//   hemv    (quaternion Hermitian mat-vec of the panel-start trailing matrix
+//            with w = f x formed on the fly, lower triangles of A and B only,
+//            per-tile deterministic partials; extra CTAs form the dot-product
+//            partials of w against the panel's previous W, Y)
 //   hreduce (sum tile partials and the dot partials, subtract the
-//            deferred-update corrections -> g; partials of c)
+//            deferred-update corrections -> g; partials of c; w written in
+//            place of x)
 // The kernels are launched with programmatic dependent launch (each starts
 // with pdl_wait), so a kernel's launch overlaps the tail of the previous one.
 // All arithmetic is FP64 (template R = double) for the plain path; the same
@@ -50,6 +53,91 @@ constexpr int RB = 32;        // rows per CTA for the row-parallel kernels
 constexpr int NG = 8;         // reflector groups per CTA in the row kernels (NT / RB)
 constexpr int TB = 64;        // tile edge of the trailing update
 constexpr int NT = 256;       // threads per CTA
+
+// ----------------------------------------------------------------------------
+// reflector head of column j (warp 0 of one CTA): combines the colupd norm
+// partials into nu = |x| and, with x_1 = (scal[0..3]), forms
+//   f = 1 / sqrt(nu (nu + |x_1|)),  head of w = f (1 + nu/|x_1|) x_1,
+//   e_j = -(nu/|x_1|) x_1  (x_1 = 0: head f nu, e_j = -nu; x = 0: no reflector),
+// written to scal[4] (f), scal[5..8] (f m), e[4j..4j+3] and tau[j]. The reads
+// bypass L1: the partials come from other CTAs of the running grid.
+// ----------------------------------------------------------------------------
+template <typename R>
+__device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
+  const int lane = threadIdx.x;
+  const int L = v.n - 1 - j;
+  if (lane >= 32 || L < 1) return;  // the last column has no subdiagonal entry
+  const double qa0 = __ldcg(v.scal + 0), qa1 = __ldcg(v.scal + 1), qb0 = __ldcg(v.scal + 2), qb1 = __ldcg(v.scal + 3);
+  // nu = scale * sqrt(sum of ssq_i (s_i / scale)^2), scale = max s_i: up to
+  // 256 partials are loaded once into registers (one memory latency, one
+  // division); more fall back to two passes over memory
+  constexpr int PL = 8;
+  double sc = 0.0, sq = 0.0;
+  if (nnp <= 32 * PL) {
+    double ps[PL], pq[PL];
+#pragma unroll
+    for (int u = 0; u < PL; ++u) {
+      const int i = lane + 32 * u;
+      ps[u] = (i < nnp) ? __ldcg(v.npart + 2 * i) : 0.0;
+      pq[u] = (i < nnp) ? __ldcg(v.npart + 2 * i + 1) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < PL; ++u) sc = fmax(sc, ps[u]);
+    sc = warp_max(sc);
+    const double inv = sc > 0.0 ? 1.0 / sc : 0.0;
+#pragma unroll
+    for (int u = 0; u < PL; ++u) { const double q = ps[u] * inv; sq += pq[u] * q * q; }
+  } else {
+    for (int i = lane; i < nnp; i += 32) sc = fmax(sc, __ldcg(v.npart + 2 * i));
+    sc = warp_max(sc);
+    const double inv = sc > 0.0 ? 1.0 / sc : 0.0;
+    for (int i = lane; i < nnp; i += 32) {
+      const double q = __ldcg(v.npart + 2 * i) * inv;
+      sq += __ldcg(v.npart + 2 * i + 1) * q * q;
+    }
+  }
+  sq = warp_sum(sq);
+  const double nu = sc * sqrt(sq);
+  if (lane != 0) return;
+  const double q1 = sqrt(qa0 * qa0 + qa1 * qa1 + qb0 * qb0 + qb1 * qb1);
+  double f = 0.0, m[4] = {0.0, 0.0, 0.0, 0.0};
+  double ee[4] = {qa0, qa1, qb0, qb1};   // L == 1: the entry itself is e_j
+  if (L >= 2) {
+    if (nu > 0.0) {
+      if (q1 > 0.0) {
+        const double s = nu / q1;
+        f = 1.0 / (sqrt(nu) * sqrt(nu + q1));
+        m[0] = qa0 * (1.0 + s); m[1] = qa1 * (1.0 + s); m[2] = qb0 * (1.0 + s); m[3] = qb1 * (1.0 + s);
+        ee[0] = -s * qa0; ee[1] = -s * qa1; ee[2] = -s * qb0; ee[3] = -s * qb1;
+      } else {
+        f = 1.0 / nu;
+        m[0] = nu;
+        ee[0] = -nu; ee[1] = 0.0; ee[2] = 0.0; ee[3] = 0.0;
+      }
+    } else {
+      ee[0] = ee[1] = ee[2] = ee[3] = 0.0;  // x == 0: nothing to reduce
+    }
+  }
+  v.scal[4] = f;
+  for (int q = 0; q < 4; ++q) v.scal[5 + q] = m[q] * f;
+  for (int q = 0; q < 4; ++q) v.e[4 * j + q] = ee[q];
+  v.tau[j] = (f > 0.0) ? 1.0 : 0.0;
+}
+
+// w at row r of column j from x (= the stored column before hreduce writes w):
+// the head row j+1 takes f m, the others f x; no reflector (f = 0) gives 0.
+template <typename R>
+__device__ __forceinline__ void w_from_x(const double* h, int r, int j, cplx<R>& wa, cplx<R>& wb) {
+  const double f = h[0];
+  if (!(f > 0.0)) { wa = czero<cplx<R>>(); wb = czero<cplx<R>>(); return; }
+  if (r == j + 1) {
+    wa = mk((R)h[1], (R)h[2]);
+    wb = mk((R)h[3], (R)h[4]);
+  } else {
+    wa = cscale(wa, (R)f);
+    wb = cscale(wb, (R)f);
+  }
+}
 
 // ----------------------------------------------------------------------------
 // colupd: rows [j, n) of column j
@@ -70,58 +158,79 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   __shared__ Z s_sc[4 * 64];        // per i: ya_i[j], yb_i[j], wa_i[j], wb_i[j]
   __shared__ Z s_red[NG][RB][2];
   __shared__ double s_red_d[2][NT / 32];
-  __shared__ double s_c;
 
-  // c_{k-1} = sum of partials (deterministic order)
-  if (k > 0 && tid < 32) {
-    double c = 0;
-    for (int i = tid; i < ncp; i += 32) c += v.cpart[i];
-    c = warp_sum(c);
-    if (tid == 0) s_c = c;
+  // Every load that does not depend on c_{k-1} is issued first, so the kernel
+  // waits about one memory latency instead of one per phase. Reflector i of
+  // the panel contributes through (w_i, y_i); y_{k-1} = g - (c/2) w_{k-1} is
+  // formed once c is known.
+  const bool live = r < n;
+  // (1) y_{k-1} on this CTA's rows: w_{k-1} and g
+  Z fwa = czero<Z>(), fwb = czero<Z>(), fga = czero<Z>(), fgb = czero<Z>();
+  if (k > 0 && grp == 0 && live) {
+    fwa = A[r + (int64_t)(j - 1) * ld]; fwb = B[r + (int64_t)(j - 1) * ld];
+    fga = v.ga[r]; fgb = v.gb[r];
   }
-  __syncthreads();
-  const R half_c = (k > 0) ? (R)(0.5 * s_c) : (R)0;
+  // (2) row-j scalars of reflector tid
+  Z cwa = czero<Z>(), cwb = czero<Z>(), cya = czero<Z>(), cyb = czero<Z>();
+  if (do_update && tid < k) {
+    cwa = A[j + (int64_t)(p + tid) * ld]; cwb = B[j + (int64_t)(p + tid) * ld];
+    if (tid == k - 1) { cya = v.ga[j]; cyb = v.gb[j]; }
+    else { cya = v.Ya[j + (int64_t)tid * v.ldy]; cyb = v.Yb[j + (int64_t)tid * v.ldy]; }
+  }
+  // (3) this row's entries of the group's first two reflectors (i = grp, grp + NG)
+  Z pw[2][2], py[2][2];
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int i = grp + u * NG;
+    pw[u][0] = pw[u][1] = py[u][0] = py[u][1] = czero<Z>();
+    if (do_update && live && i < k) {
+      pw[u][0] = A[r + (int64_t)(p + i) * ld]; pw[u][1] = B[r + (int64_t)(p + i) * ld];
+      if (i == k - 1) { py[u][0] = v.ga[r]; py[u][1] = v.gb[r]; }
+      else { py[u][0] = v.Ya[r + (int64_t)i * v.ldy]; py[u][1] = v.Yb[r + (int64_t)i * v.ldy]; }
+    }
+  }
+  // (4) the column itself
+  Z x0a = czero<Z>(), x0b = czero<Z>();
+  if (do_update && grp == 0 && live) { x0a = A[r + (int64_t)j * ld]; x0b = B[r + (int64_t)j * ld]; }
+  // (5) c_{k-1} = sum of the previous column's partials (deterministic order)
+  double cl = 0.0;
+  if (k > 0)
+    for (int i = tid; i < ncp; i += NT) cl += v.cpart[i];
+  const double csum = (k > 0) ? block_sum(cl, s_red_d[0]) : 0.0;
+  const R half_c = (R)(0.5 * csum);
 
   // finish y_{k-1} = g - (c/2) w_{k-1} on this CTA's rows (rows >= j)
-  if (k > 0 && grp == 0 && r < n) {
-    const Z wa = A[r + (int64_t)(j - 1) * ld], wb = B[r + (int64_t)(j - 1) * ld];
-    v.Ya[r + (int64_t)(k - 1) * v.ldy] = csub(v.ga[r], cscale(wa, half_c));
-    v.Yb[r + (int64_t)(k - 1) * v.ldy] = csub(v.gb[r], cscale(wb, half_c));
+  if (k > 0 && grp == 0 && live) {
+    v.Ya[r + (int64_t)(k - 1) * v.ldy] = csub(fga, cscale(fwa, half_c));
+    v.Yb[r + (int64_t)(k - 1) * v.ldy] = csub(fgb, cscale(fwb, half_c));
   }
   if (!do_update) return;
 
-  // scalars at row j for every previous reflector of the panel
-  for (int i = tid; i < k; i += NT) {
-    Z ya, yb;
-    const Z wa = A[j + (int64_t)(p + i) * ld], wb = B[j + (int64_t)(p + i) * ld];
-    if (i == k - 1) {
-      ya = csub(v.ga[j], cscale(wa, half_c));
-      yb = csub(v.gb[j], cscale(wb, half_c));
-    } else {
-      ya = v.Ya[j + (int64_t)i * v.ldy];
-      yb = v.Yb[j + (int64_t)i * v.ldy];
-    }
-    s_sc[4 * i + 0] = ya; s_sc[4 * i + 1] = yb; s_sc[4 * i + 2] = wa; s_sc[4 * i + 3] = wb;
+  // scalars at row j for every previous reflector of the panel (k <= nbmax = 64 < NT)
+  if (tid < k) {
+    if (tid == k - 1) { cya = csub(cya, cscale(cwa, half_c)); cyb = csub(cyb, cscale(cwb, half_c)); }
+    s_sc[4 * tid + 0] = cya; s_sc[4 * tid + 1] = cyb; s_sc[4 * tid + 2] = cwa; s_sc[4 * tid + 3] = cwb;
   }
   __syncthreads();
 
   Z da = czero<Z>(), db = czero<Z>();
-  if (r < n) {
-    for (int i = grp; i < k; i += NG) {
-      const Z sya = s_sc[4 * i + 0], syb = s_sc[4 * i + 1], swa = s_sc[4 * i + 2], swb = s_sc[4 * i + 3];
+  auto contrib = [&](int i, Z wa, Z wb, Z ya, Z yb) {
+    const Z sya = s_sc[4 * i + 0], syb = s_sc[4 * i + 1], swa = s_sc[4 * i + 2], swb = s_sc[4 * i + 3];
+    if (i == k - 1) { ya = csub(ya, cscale(wa, half_c)); yb = csub(yb, cscale(wb, half_c)); }
+    // A part: wa conj(ya_j) + conj(wb) yb_j + ya conj(wa_j) + conj(yb) wb_j
+    cfmacb(da, wa, sya); cfmac(da, wb, syb); cfmacb(da, ya, swa); cfmac(da, yb, swb);
+    // B part: wb conj(ya_j) - conj(wa) yb_j + yb conj(wa_j) - conj(ya) wb_j
+    cfmacb(db, wb, sya); cfmac(db, cneg(wa), syb); cfmacb(db, yb, swa); cfmac(db, cneg(ya), swb);
+  };
+  if (live) {
+    if (grp < k) contrib(grp, pw[0][0], pw[0][1], py[0][0], py[0][1]);
+    if (grp + NG < k) contrib(grp + NG, pw[1][0], pw[1][1], py[1][0], py[1][1]);
+    for (int i = grp + 2 * NG; i < k; i += NG) {  // panels wider than 16
       const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
       Z ya, yb;
-      if (i == k - 1) {
-        ya = csub(v.ga[r], cscale(wa, half_c));
-        yb = csub(v.gb[r], cscale(wb, half_c));
-      } else {
-        ya = v.Ya[r + (int64_t)i * v.ldy];
-        yb = v.Yb[r + (int64_t)i * v.ldy];
-      }
-      // A part: wa conj(ya_j) + conj(wb) yb_j + ya conj(wa_j) + conj(yb) wb_j
-      cfmacb(da, wa, sya); cfmac(da, wb, syb); cfmacb(da, ya, swa); cfmac(da, yb, swb);
-      // B part: wb conj(ya_j) - conj(wa) yb_j + yb conj(wa_j) - conj(ya) wb_j
-      cfmacb(db, wb, sya); cfmac(db, cneg(wa), syb); cfmacb(db, yb, swa); cfmac(db, cneg(ya), swb);
+      if (i == k - 1) { ya = v.ga[r]; yb = v.gb[r]; }
+      else { ya = v.Ya[r + (int64_t)i * v.ldy]; yb = v.Yb[r + (int64_t)i * v.ldy]; }
+      contrib(i, wa, wb, ya, yb);
     }
   }
   s_red[grp][row][0] = da;
@@ -133,14 +242,15 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   if (grp == 0 && r < n) {
     Z ta = s_red[0][row][0], tb = s_red[0][row][1];
     for (int g2 = 1; g2 < NG; ++g2) { ta = cadd(ta, s_red[g2][row][0]); tb = cadd(tb, s_red[g2][row][1]); }
-    xa = csub(A[r + (int64_t)j * ld], ta);
-    xb = csub(B[r + (int64_t)j * ld], tb);
+    xa = csub(x0a, ta);
+    xb = csub(x0b, tb);
     A[r + (int64_t)j * ld] = xa;
     B[r + (int64_t)j * ld] = xb;
     if (r == j) v.d[j] = (double)xa.x;
     if (r == j + 1) {
       v.scal[0] = (double)xa.x; v.scal[1] = (double)xa.y;
       v.scal[2] = (double)xb.x; v.scal[3] = (double)xb.y;
+      __threadfence();  // before this CTA's arrival is counted
     }
     if (r > j) {
       sc = fmax(fmax(fabs((double)xa.x), fabs((double)xa.y)), fmax(fabs((double)xb.x), fabs((double)xb.y)));
@@ -155,124 +265,126 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
     ss = a0 * a0 + a1 * a1 + b0 * b0 + b1 * b1;
   }
   const double bss = block_sum(ss, s_red_d[1]);
+  __shared__ bool s_last;
   if (tid == 0) {
     v.npart[2 * blockIdx.x + 0] = bmax;
     v.npart[2 * blockIdx.x + 1] = bss;
+    __threadfence();
+    s_last = atomicAdd(v.counter, 1u) == gridDim.x - 1;
   }
+  __syncthreads();
+  if (!s_last) return;
+  // every CTA's partials (and x_1) are visible: form the reflector head once
+  __threadfence();
+  reflector_head(v, j, gridDim.x);
+  if (tid == 0) *v.counter = 0u;
 }
 
 // ----------------------------------------------------------------------------
-// reflect: rows [j+1, n); builds w in place of x, writes e_j, dot partials.
+// dot partials of w (rows [j+1, n)) against the panel's previous reflectors
+// and aux vectors, DR rows per CTA (warp = 32 rows, lane = row):
+//   <y_i,w> = ya^H wa + yb^H wb,  [y_i,w] = ya^T wb - yb^T wa,  same for w_i.
+// The warps' sums meet in `scratch` (4 warps x k x 4) and the CTA writes one
+// partial per (i, product).
 // ----------------------------------------------------------------------------
+constexpr int DR = 128;       // rows per dot-partial CTA
 template <typename R>
-__global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, int k, int nnp) {
-  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+__device__ void panel_dots(const TridiagView<R>& v, int p, int j, int k, int b, int ndot, cplx<R>* scratch) {
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
-  Z* A = v.M;
-  Z* B = v.M + n;
-  const int L = n - 1 - j;
-  const int tid = threadIdx.x;
-  __shared__ double s_sc[5];  // f, first element of w (a.re, a.im, b.re, b.im)
-  double nu = 0.0;
-  if (tid < 32) {
-    // combine norm partials: nu = scale * sqrt(ssq)
-    double scale = 0.0;
-    for (int i = tid; i < nnp; i += 32) scale = fmax(scale, v.npart[2 * i]);
-    scale = warp_max(scale);
-    double ssq = 0.0;
-    if (scale > 0.0)
-      for (int i = tid; i < nnp; i += 32) {
-        const double si = v.npart[2 * i];
-        if (si > 0.0) { const double q = si / scale; ssq += v.npart[2 * i + 1] * q * q; }
-      }
-    ssq = warp_sum(ssq);
-    nu = scale * sqrt(ssq);
+  const Z* A = v.M;
+  const Z* B = v.M + n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gr = j + 1 + b * DR + warp * 32 + lane;
+  const bool live = gr < n;
+  double h[5];
+  Z xa = czero<Z>(), xb = czero<Z>();
+  if (live) {
+#pragma unroll
+    for (int u = 0; u < 5; ++u) h[u] = v.scal[4 + u];
+    xa = A[gr + (int64_t)j * ld];
+    xb = B[gr + (int64_t)j * ld];
   }
-  if (tid == 0) {
-    const double qa0 = v.scal[0], qa1 = v.scal[1], qb0 = v.scal[2], qb1 = v.scal[3];
-    const double q1 = sqrt(qa0 * qa0 + qa1 * qa1 + qb0 * qb0 + qb1 * qb1);
-    double f = 0.0, m[4] = {0.0, 0.0, 0.0, 0.0};
-    double ee[4] = {qa0, qa1, qb0, qb1};   // L == 1: the entry itself is e_j
-    if (L >= 2) {
-      if (nu > 0.0) {
-        if (q1 > 0.0) {
-          const double s = nu / q1;
-          f = 1.0 / (sqrt(nu) * sqrt(nu + q1));
-          m[0] = qa0 * (1.0 + s); m[1] = qa1 * (1.0 + s); m[2] = qb0 * (1.0 + s); m[3] = qb1 * (1.0 + s);
-          ee[0] = -s * qa0; ee[1] = -s * qa1; ee[2] = -s * qb0; ee[3] = -s * qb1;
-        } else {
-          f = 1.0 / nu;
-          m[0] = nu;
-          ee[0] = -nu; ee[1] = 0.0; ee[2] = 0.0; ee[3] = 0.0;
-        }
-      } else {
-        ee[0] = ee[1] = ee[2] = ee[3] = 0.0;  // x == 0: nothing to reduce
+  Z ya[4], yb[4], qa[4], qb[4];
+  for (int i0 = 0; i0 < k; i0 += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      ya[u] = yb[u] = qa[u] = qb[u] = czero<Z>();
+      if (live && i < k) {
+        ya[u] = v.Ya[gr + (int64_t)i * v.ldy]; yb[u] = v.Yb[gr + (int64_t)i * v.ldy];
+        qa[u] = A[gr + (int64_t)(p + i) * ld]; qb[u] = B[gr + (int64_t)(p + i) * ld];
       }
     }
-    s_sc[0] = f;
-    for (int q = 0; q < 4; ++q) s_sc[1 + q] = m[q] * f;
-    if (blockIdx.x == 0) {
-      for (int q = 0; q < 4; ++q) v.e[4 * j + q] = ee[q];
-      v.tau[j] = (f > 0.0) ? 1.0 : 0.0;
+    if (i0 == 0 && live) w_from_x<R>(h, gr, j, xa, xb);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u;
+      if (i >= k) break;
+      Z d1 = czero<Z>(), d2 = czero<Z>(), d3 = czero<Z>(), d4 = czero<Z>();
+      cfmac(d1, ya[u], xa); cfmac(d1, yb[u], xb);
+      cfma(d2, ya[u], xb); cfma(d2, cneg(yb[u]), xa);
+      cfmac(d3, qa[u], xa); cfmac(d3, qb[u], xb);
+      cfma(d4, qa[u], xb); cfma(d4, cneg(qb[u]), xa);
+      d1.x = warp_sum(d1.x); d1.y = warp_sum(d1.y);
+      d2.x = warp_sum(d2.x); d2.y = warp_sum(d2.y);
+      d3.x = warp_sum(d3.x); d3.y = warp_sum(d3.y);
+      d4.x = warp_sum(d4.x); d4.y = warp_sum(d4.y);
+      if (lane == 0) {
+        Z* o = scratch + ((int64_t)warp * k + i) * 4;
+        o[0] = d1; o[1] = d2; o[2] = d3; o[3] = d4;
+      }
     }
   }
   __syncthreads();
-  const double f = s_sc[0];
-  const int r0 = j + 1 + blockIdx.x * RB;
-  const int row = tid & (RB - 1);
-  const int grp = tid >> 5;
-  const int r = r0 + row;
-  __shared__ Z s_wa[RB], s_wb[RB];
-  if (grp == 0) {
-    Z wa = czero<Z>(), wb = czero<Z>();
-    if (r < n) {
-      if (f > 0.0) {
-        if (r == j + 1) {
-          wa = mk((R)s_sc[1], (R)s_sc[2]);
-          wb = mk((R)s_sc[3], (R)s_sc[4]);
-        } else {
-          wa = cscale(A[r + (int64_t)j * ld], (R)f);
-          wb = cscale(B[r + (int64_t)j * ld], (R)f);
-        }
-      }
-      A[r + (int64_t)j * ld] = wa;
-      B[r + (int64_t)j * ld] = wb;
-    }
-    s_wa[row] = wa; s_wb[row] = wb;
+  for (int t = threadIdx.x; t < 4 * k; t += blockDim.x) {
+    Z acc = scratch[t];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) acc = cadd(acc, scratch[w * 4 * k + t]);
+    v.dpart[((int64_t)b * v.nbmax + (t >> 2)) * 4 + (t & 3)] = acc;
   }
-  // dot partials vs previous reflectors / aux vectors of the panel
-  if (k == 0 || L < 2) return;
+  // the last dot CTA to finish sums all ndot partials into dots (fixed order:
+  // nsplit threads per output over interleaved partials, then combined in order)
+  __threadfence();
+  __shared__ unsigned s_ticket;
   __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
-  const int gr = r0 + lane;
-  const Z xa = s_wa[lane], xb = s_wb[lane];
-  for (int i = warp; i < k; i += NT / 32) {
-    Z d1 = czero<Z>(), d2 = czero<Z>(), d3 = czero<Z>(), d4 = czero<Z>();
-    if (gr < n) {
-      const Z ya = v.Ya[gr + (int64_t)i * v.ldy], yb = v.Yb[gr + (int64_t)i * v.ldy];
-      const Z qa = A[gr + (int64_t)(p + i) * ld], qb = B[gr + (int64_t)(p + i) * ld];
-      // <y,w> = ya^H xa + yb^H xb ; [y,w] = ya^T xb - yb^T xa
-      cfmac(d1, ya, xa); cfmac(d1, yb, xb);
-      cfma(d2, ya, xb); cfma(d2, cneg(yb), xa);
-      cfmac(d3, qa, xa); cfmac(d3, qb, xb);
-      cfma(d4, qa, xb); cfma(d4, cneg(qb), xa);
+  if (threadIdx.x == 0) s_ticket = atomicAdd(v.counter + 1, 1u);
+  __syncthreads();
+  if (s_ticket != (unsigned)(ndot - 1)) return;
+  __threadfence();
+  const int no = 4 * k;
+  if (no > (int)blockDim.x) {  // panels wider than 32: one thread per output
+    for (int o = threadIdx.x; o < no; o += blockDim.x) {
+      Z d = czero<Z>();
+#pragma unroll 8
+      for (int c = 0; c < ndot; ++c) d = cadd(d, __ldcg(v.dpart + ((int64_t)c * v.nbmax + (o >> 2)) * 4 + (o & 3)));
+      v.dots[o] = d;
     }
-    d1.x = warp_sum(d1.x); d1.y = warp_sum(d1.y);
-    d2.x = warp_sum(d2.x); d2.y = warp_sum(d2.y);
-    d3.x = warp_sum(d3.x); d3.y = warp_sum(d3.y);
-    d4.x = warp_sum(d4.x); d4.y = warp_sum(d4.y);
-    if (lane == 0) {
-      Z* o = v.dpart + ((int64_t)blockIdx.x * v.nbmax + i) * 4;
-      o[0] = d1; o[1] = d2; o[2] = d3; o[3] = d4;
+  } else {
+    const int nsplit = (int)blockDim.x / no;
+    const int t = threadIdx.x % no, sp = threadIdx.x / no;
+    Z acc = czero<Z>();
+    if (sp < nsplit) {
+#pragma unroll 8
+      for (int c = sp; c < ndot; c += nsplit)
+        acc = cadd(acc, __ldcg(v.dpart + ((int64_t)c * v.nbmax + (t >> 2)) * 4 + (t & 3)));
+    }
+    __syncthreads();  // scratch is free again
+    scratch[threadIdx.x] = acc;
+    __syncthreads();
+    if ((int)threadIdx.x < no) {
+      Z d = scratch[threadIdx.x];
+      for (int u = 1; u < nsplit; ++u) d = cadd(d, scratch[u * no + threadIdx.x]);
+      v.dots[threadIdx.x] = d;
     }
   }
+  if (threadIdx.x == 0) v.counter[1] = 0u;
 }
 
 // ----------------------------------------------------------------------------
 // hemv: quaternion Hermitian mat-vec of the panel-start trailing matrix.
-//   Region rows/cols [r0, n); lower-triangle 32x32 tiles, one CTA per tile.
+//   Region rows/cols [r0, n); lower-triangle 32x32 tiles, one CTA per tile
+//   after the first ndot CTAs, which form the panel dot partials.
 //   The A and B tiles are staged in shared memory (padded, conflict-free for
 //   both row and column sweeps) and four warps each own one product:
 //     warp 0: rows,  A x and A z          warp 2: columns, A^H x and A^H z
@@ -286,7 +398,7 @@ __global__ void __launch_bounds__(NT) k_reflect(TridiagView<R> v, int p, int j, 
 constexpr int HT = 32;        // hemv tile edge
 constexpr int HLD = HT + 1;   // padded shared leading dimension
 template <typename R>
-__global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
+__global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int p, int j, int k, int ndot) {
   pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
@@ -294,34 +406,63 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
   const Z* A = v.M;
   const Z* B = v.M + n;
   const int r0 = j + 1;
-  const int t = blockIdx.x;
+  __shared__ Z sA[HT * HLD], sB[HT * HLD];
+  __shared__ Z sx[2][HT], sz[2][HT];   // [0]: rows of block I, [1]: rows of block J
+  __shared__ Z sout[HT][4];
+  // the first ndot CTAs form the panel dot partials (they start first and run
+  // beside the tiles); sA (HT * HLD >= 4 warps x 64 x 4) is their scratch
+  if ((int)blockIdx.x < ndot) {
+    panel_dots(v, p, j, k, blockIdx.x, ndot, sA);
+    return;
+  }
+  const int t = blockIdx.x - ndot;
   int I, J;
   tri_tile(t, I, J);
   const bool diag = (I == J);
   const int tid = threadIdx.x;
   const int rbase = r0 + I * HT, cbase = r0 + J * HT;
-  __shared__ Z sA[HT * HLD], sB[HT * HLD];
-  __shared__ Z sx[2][HT], sz[2][HT];   // [0]: rows of block I, [1]: rows of block J
-  __shared__ Z sout[HT][4];
-  for (int e = tid; e < HT * HT; e += 128) {
+  // all of this thread's loads are issued before any is used: 8 elements of
+  // each tile (one column of 32 rows per warp and step: coalesced), the two
+  // w segments and the reflector head
+  constexpr int PER = HT * HT / 128;
+  Z ta[PER], tb[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = tid + 128 * u;
     const int r = e & (HT - 1), c = e >> 5;
     const int gr = rbase + r, gc = cbase + c;
-    Z a = czero<Z>(), b = czero<Z>();
+    ta[u] = czero<Z>(); tb[u] = czero<Z>();
     if (gr < n && gc < n && (!diag || r >= c)) {
-      a = A[gr + (int64_t)gc * ld];
-      b = B[gr + (int64_t)gc * ld];
-      if (diag && r == c) { a.y = 0; b = czero<Z>(); }
+      ta[u] = A[gr + (int64_t)gc * ld];
+      tb[u] = B[gr + (int64_t)gc * ld];
     }
-    sA[r + c * HLD] = a;
-    sB[r + c * HLD] = b;
+  }
+  const int ws = tid >> 5, wq = tid & (HT - 1);
+  const int wg = (ws == 0 ? rbase : cbase) + wq;
+  const bool wrow = tid < 2 * HT && wg < n;
+  Z x = czero<Z>(), z = czero<Z>();
+  double h[5];
+  if (wrow) {
+#pragma unroll
+    for (int u = 0; u < 5; ++u) h[u] = v.scal[4 + u];
+    x = A[wg + (int64_t)j * ld];
+    z = B[wg + (int64_t)j * ld];
+  }
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = tid + 128 * u;
+    const int r = e & (HT - 1), c = e >> 5;
+    if (diag && r == c) { ta[u].y = 0; tb[u] = czero<Z>(); }
+    sA[r + c * HLD] = ta[u];
+    sB[r + c * HLD] = tb[u];
   }
   if (tid < 2 * HT) {
-    const int s = tid >> 5, q = tid & (HT - 1);
-    const int g = (s == 0 ? rbase : cbase) + q;
-    Z x = czero<Z>(), z = czero<Z>();
-    if (g < n) { x = A[g + (int64_t)j * ld]; z = cconj(B[g + (int64_t)j * ld]); }
-    sx[s][q] = x;
-    sz[s][q] = z;
+    if (wrow) {
+      w_from_x<R>(h, wg, j, x, z);
+      z = cconj(z);
+    }
+    sx[ws][wq] = x;
+    sz[ws][wq] = z;
   }
   __syncthreads();
   const int role = tid >> 5, q = tid & (HT - 1);
@@ -368,83 +509,88 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int j) {
 }
 
 // ----------------------------------------------------------------------------
-// hreduce: g = H_panelstart w - corrections, for rows [j+1, n); c partials.
+// hreduce: g = H_panelstart w - corrections, for rows [j+1, n); c partials;
+//   w = f x written in place of x.
 //   T is the hemv tile edge used for this column; nblk its number of blocks.
-//   HRB rows per CTA; four threads per (row, product) sum the hemv tile
-//   partials (fixed split and combine order: deterministic). Every CTA also
-//   sums the reflect kernel's dot partials (ndp of them) itself, in the same
-//   fixed order, so no separate reduction launch sits between reflect and hemv.
+//   HRB rows per CTA; NSPL threads per (row, product) sum the hemv tile
+//   partials (fixed split and combine order: deterministic). The panel dot
+//   products come finished from the hemv grid (dots). All loads that do not
+//   depend on one another are issued before the first is used.
 // ----------------------------------------------------------------------------
-constexpr int HRB = 16;          // rows per CTA
-constexpr int HNG = NT / HRB;    // reflector groups for the corrections
+constexpr int HRB = 8;                 // rows per CTA
+constexpr int HNG = NT / HRB;          // reflector groups for the corrections
+constexpr int NSPL = NT / (4 * HRB);   // threads per (row, product) for the tile partials
 template <typename R>
-__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode,
-                                                int ndp) {
+__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode) {
   pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
-  const Z* A = v.M;
-  const Z* B = v.M + n;
+  Z* A = v.M;
+  Z* B = v.M + n;
   const int r0 = j + 1;
   const int tid = threadIdx.x;
-  const int row = tid & (HRB - 1), grp = tid >> 4;
-  const int lrow = blockIdx.x * HRB + row;   // row index inside the region
-  const int r = r0 + lrow;
+  const int row = tid & (HRB - 1), grp = tid / HRB;
+  const int r = r0 + blockIdx.x * HRB + row;
   __shared__ Z s_v[HRB][4];
   __shared__ Z s_dots[4 * 64];
-  __shared__ Z s_part[4][4 * HRB];
-  __shared__ Z s_dsub[NT];
+  __shared__ Z s_part[NSPL][4 * HRB];
   __shared__ Z s_red[HNG][HRB][2];
   __shared__ double s_redd[NT / 32];
+  // this row's x and the reflector head (w = f x is written in place at the end)
+  double h[5];
+  Z xa = czero<Z>(), xb = czero<Z>();
+  if (grp == 0 && r < n) {
+#pragma unroll
+    for (int u = 0; u < 5; ++u) h[u] = v.scal[4 + u];
+    xa = A[r + (int64_t)j * ld];
+    xb = B[r + (int64_t)j * ld];
+  }
+  // the group's first reflector (w_i, y_i) at this row, and the panel dots
+  Z cwa = czero<Z>(), cwb = czero<Z>(), cya = czero<Z>(), cyb = czero<Z>(), dt = czero<Z>();
   if (!zero_mode) {
-    // (1) tile partials: output o = (row, product), quarter q sums blocks S = q, q + 4, ...
-    const int o = tid & (4 * HRB - 1), quarter = tid >> 6;
-    const int orow = o >> 2, ou = o & 3;
-    const int lr = blockIdx.x * HRB + orow;
-    Z s0 = czero<Z>(), s1 = czero<Z>();
+    if (r < n && grp < k) {
+      cwa = A[r + (int64_t)(p + grp) * ld]; cwb = B[r + (int64_t)(p + grp) * ld];
+      cya = v.Ya[r + (int64_t)grp * v.ldy]; cyb = v.Yb[r + (int64_t)grp * v.ldy];
+    }
+    if (tid < 4 * k) dt = v.dots[tid];
+    // tile partials: output o = (row, product); split sp sums blocks S = sp, sp + NSPL, ...
+    const int o = tid & (4 * HRB - 1), sp = tid / (4 * HRB);
+    const int lr = blockIdx.x * HRB + (o >> 2);
+    Z s0 = czero<Z>(), s1 = czero<Z>(), s2 = czero<Z>(), s3 = czero<Z>();
     if (r0 + lr < n) {
       const int Rb = lr / T, off = lr % T;
-      const int nbm = v.hblk;
-      const Z* base = v.hpart + (((int64_t)Rb * nbm) * T + off) * 4 + ou;
+      const Z* base = v.hpart + (((int64_t)Rb * v.hblk) * T + off) * 4 + (o & 3);
       const int64_t stride = (int64_t)T * 4;
-      int S = quarter;
-      for (; S + 4 < nblk; S += 8) { s0 = cadd(s0, base[S * stride]); s1 = cadd(s1, base[(S + 4) * stride]); }
-      for (; S < nblk; S += 4) s0 = cadd(s0, base[S * stride]);
-    }
-    s_part[quarter][o] = cadd(s0, s1);
-    // (2) dot products of the panel: 4k outputs, the ndp partials split over NT / 4k threads each
-    if (k > 0) {
-      const int no = 4 * k;
-      const int nsub = NT / no;
-      const int t = tid % no, sub = tid / no;
-      Z acc = czero<Z>();
-      if (sub < nsub) {
-        const int i = t >> 2, q = t & 3;
-        for (int c = sub; c < ndp; c += nsub) acc = cadd(acc, v.dpart[((int64_t)c * v.nbmax + i) * 4 + q]);
+      int S = sp;
+#pragma unroll 2
+      for (; S + 3 * NSPL < nblk; S += 4 * NSPL) {
+        const Z a0 = base[S * stride], a1 = base[(S + NSPL) * stride], a2 = base[(S + 2 * NSPL) * stride],
+                a3 = base[(S + 3 * NSPL) * stride];
+        s0 = cadd(s0, a0); s1 = cadd(s1, a1); s2 = cadd(s2, a2); s3 = cadd(s3, a3);
       }
-      s_dsub[tid] = acc;
+      for (; S < nblk; S += NSPL) s0 = cadd(s0, base[S * stride]);
     }
+    s_part[sp][o] = cadd(cadd(s0, s2), cadd(s1, s3));
+    if (tid < 4 * k) s_dots[tid] = dt;
   }
   __syncthreads();
-  if (!zero_mode) {
-    if (tid < 4 * HRB)
-      s_v[tid >> 2][tid & 3] = cadd(cadd(s_part[0][tid], s_part[1][tid]), cadd(s_part[2][tid], s_part[3][tid]));
-    if (k > 0 && tid < 4 * k) {
-      const int no = 4 * k, nsub = NT / no;
-      Z d = s_dsub[tid];
-      for (int sub = 1; sub < nsub; ++sub) d = cadd(d, s_dsub[sub * no + tid]);
-      s_dots[tid] = d;
-    }
+  if (!zero_mode && tid < 4 * HRB) {
+    Z t = s_part[0][tid];
+#pragma unroll
+    for (int u = 1; u < NSPL; ++u) t = cadd(t, s_part[u][tid]);
+    s_v[tid >> 2][tid & 3] = t;
   }
-  __syncthreads();
   // deferred-update corrections, reflectors split over the groups
   Z ta = czero<Z>(), tb = czero<Z>();
   if (!zero_mode && r < n) {
     for (int i = grp; i < k; i += HNG) {
+      Z wa = cwa, wb = cwb, ya = cya, yb = cyb;
+      if (i != grp) {
+        wa = A[r + (int64_t)(p + i) * ld]; wb = B[r + (int64_t)(p + i) * ld];
+        ya = v.Ya[r + (int64_t)i * v.ldy]; yb = v.Yb[r + (int64_t)i * v.ldy];
+      }
       const Z s1 = s_dots[4 * i + 0], s2 = s_dots[4 * i + 1], s3 = s_dots[4 * i + 2], s4 = s_dots[4 * i + 3];
-      const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
-      const Z ya = v.Ya[r + (int64_t)i * v.ldy], yb = v.Yb[r + (int64_t)i * v.ldy];
       // ga -= wa s1 - conj(wb) s2 + ya s3 - conj(yb) s4
       // gb -= wb s1 + conj(wa) s2 + yb s3 + conj(ya) s4
       cfma(ta, wa, s1); cfmac(ta, cneg(wb), s2); cfma(ta, ya, s3); cfmac(ta, cneg(yb), s4);
@@ -456,13 +602,17 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
   __syncthreads();
   double cp = 0.0;
   if (grp == 0 && r < n) {
+    Z wa = xa, wb = xb;
+    w_from_x<R>(h, r, j, wa, wb);
+    A[r + (int64_t)j * ld] = wa;
+    B[r + (int64_t)j * ld] = wb;
     Z ga = czero<Z>(), gb = czero<Z>();
     if (!zero_mode) {
       // ha = A x - conj(B z), hb = B x + conj(A z)
       ga = csub(s_v[row][0], cconj(s_v[row][3]));
       gb = cadd(s_v[row][2], cconj(s_v[row][1]));
-      for (int g2 = 0; g2 < HNG; ++g2) { ga = csub(ga, s_red[g2][row][0]); gb = csub(gb, s_red[g2][row][1]); }
-      const Z wa = A[r + (int64_t)j * ld], wb = B[r + (int64_t)j * ld];
+      const int ng = k < HNG ? k : HNG;   // groups that hold a correction
+      for (int g2 = 0; g2 < ng; ++g2) { ga = csub(ga, s_red[g2][row][0]); gb = csub(gb, s_red[g2][row][1]); }
       cp = (double)(wa.x * ga.x + wa.y * ga.y + wb.x * gb.x + wb.y * gb.y);
     }
     v.ga[r] = ga;
@@ -572,6 +722,7 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
   if (n <= 0) return ZQ_OK;
   if (nb > v.nbmax) nb = v.nbmax;
   if (nb < 1) nb = 1;
+  ZQ_CUDA(cudaMemsetAsync(v.counter, 0, 2 * sizeof(unsigned), st));
   int ncp = 0;  // number of c partials of the previous column
   for (int p = 0; p < n; p += nb) {
     const int nbp = (nb < n - p) ? nb : (n - p);
@@ -583,21 +734,20 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
       ZQ_CUDA(launch_pdl(k_colupd<R>, dim3(ncta1), dim3(NT), st, v, p, j, k, ncp, 1));
       count_launch();
       if (L < 1) { prof_end(PC_PANEL, st); ncp = 0; continue; }
-      const int ncta2 = ceil_div(L, RB);
-      ZQ_CUDA(launch_pdl(k_reflect<R>, dim3(ncta2), dim3(NT), st, v, p, j, k, ncta1));
-      count_launch();
       const int T = HT;
       const int nblk = ceil_div(L, T);
+      const int ndot = (k > 0 && L >= 2) ? ceil_div(L, DR) : 0;  // dot-partial CTAs of the hemv grid
       prof_end(PC_PANEL, st);
       if (L >= 2) {
         prof_begin(PC_HEMV, st);
-        ZQ_CUDA(launch_pdl(k_hemv<R>, dim3(nblk * (nblk + 1) / 2), dim3(128), st, v, j));
+        const int ntiles = nblk * (nblk + 1) / 2;
+        ZQ_CUDA(launch_pdl(k_hemv<R>, dim3(ntiles + ndot), dim3(128), st, v, p, j, k, ndot));
         count_launch();
         prof_end(PC_HEMV, st);
       }
       prof_begin(PC_PANEL, st);
       const int nhr = ceil_div(L, HRB);
-      ZQ_CUDA(launch_pdl(k_hreduce<R>, dim3(nhr), dim3(NT), st, v, p, j, k, T, nblk, L < 2 ? 1 : 0, ncta2));
+      ZQ_CUDA(launch_pdl(k_hreduce<R>, dim3(nhr), dim3(NT), st, v, p, j, k, T, nblk, L < 2 ? 1 : 0));
       count_launch();
       prof_end(PC_PANEL, st);
       ncp = nhr;
@@ -630,7 +780,9 @@ size_t tridiag_workspace_bytes(int n, int nbmax) {
   b += sizeof(Z) * ((hblk + 2) * (hblk + 2) * 32 * 4);  // hpart: 32-tiles, or 64-tiles at the same block stride
   b += sizeof(Z) * (hblk * nbmax * 4);                // dpart
   b += sizeof(Z) * (4 * (size_t)nbmax);               // dots
-  b += sizeof(double) * (4 * hblk + 8);               // npart (2 hblk), cpart (one per 16 rows), scal
+  b += sizeof(double) * (2 * hblk + 16);              // npart (2 hblk), scal
+  b += sizeof(double) * ((size_t)ceil_div(n > 0 ? n : 1, HRB) + 1);  // cpart (one per hreduce CTA)
+  b += sizeof(unsigned) * 2;                          // counters
   return b + 16 * 256;
 }
 
@@ -650,8 +802,9 @@ TridiagView<R> tridiag_bind(void* ws, cplx<R>* M, int n, int64_t ld, int nbmax, 
   v.dpart = reinterpret_cast<Z*>(take(sizeof(Z) * (size_t)hblk * nbmax * 4));
   v.dots = reinterpret_cast<Z*>(take(sizeof(Z) * 4 * (size_t)nbmax));
   v.npart = reinterpret_cast<double*>(take(sizeof(double) * 2 * hblk));
-  v.cpart = reinterpret_cast<double*>(take(sizeof(double) * 2 * hblk));
-  v.scal = reinterpret_cast<double*>(take(sizeof(double) * 8));
+  v.cpart = reinterpret_cast<double*>(take(sizeof(double) * ((size_t)ceil_div(n > 0 ? n : 1, HRB) + 1)));
+  v.scal = reinterpret_cast<double*>(take(sizeof(double) * 16));
+  v.counter = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * 2));
   v.d = d; v.e = e; v.tau = tau;
   return v;
 }
