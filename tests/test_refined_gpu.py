@@ -93,3 +93,23 @@ def test_refined_mma_sync_products(mma_sync, n):
     assert metrics.residual(h, out, eig[:n]) <= TOL
     assert metrics.orthonormality(out) <= TOL
     assert metrics.structure_exact(out, n)
+
+
+@pytest.mark.parametrize("n", [300, 700, 1500])
+def test_refined_converges_without_fallback(gpu, n):
+    """The FP32 decomposition (reduction, divide and conquer, Q formation and
+    back-transform on the FP32 GEMM kernels) is accurate enough for the
+    refinement to converge in at most three steps, without the FP64 fallback
+    that would otherwise hide an FP32 error behind a correct result."""
+    from zquatev_gb300 import solver
+
+    d = inputs.random_matrix(n, 6200 + n)
+    out, eig = refined(gpu, d, 1)
+    iters, last_corr, fell_back = solver.refine_stats()
+    assert not fell_back
+    assert 1 <= iters <= 3, iters
+    assert last_corr <= 1e-7
+    h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
+    ref = np.linalg.eigvalsh(h)[::2]
+    assert metrics.eig_error(eig[:n], ref, metrics.h_norm2(ref)) <= TOL
+    assert metrics.residual(h, out, eig[:n]) <= TOL

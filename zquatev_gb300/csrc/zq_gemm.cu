@@ -20,6 +20,8 @@
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
+#include <type_traits>
+
 namespace zq {
 
 constexpr int GT = 64;   // output tile edge
@@ -179,6 +181,243 @@ static int choose_splits(const ZgemmArgsT<R>& g) {
   return s;
 }
 
+// ----------------------------------------------------------------------------
+// FP32 kernels (the refined path's decomposition). The DFMA-shaped kernels
+// above leave FP32 bound by shared-memory loads (2 FMA per scalar load); these
+// keep the same 64 x 64 output tiles but give each thread an 8 x 8 real or a
+// 4 x 8 complex (4M: two accumulators per output) micro-tile read with 16-byte
+// shared loads (4 and 5.3 FMA per loaded float), and double-buffer 16-deep K
+// stages with cp.async (zero fill outside the matrix).
+// ----------------------------------------------------------------------------
+constexpr int SK = 16;       // k per stage
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool pred) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem), "r"(pred ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool pred) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(pred ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// complex, 64 x 64 complex tile, 128 threads (16 x 8), thread (tr, tc) owns rows
+// {2tr, 2tr+1, 32+2tr, 33+2tr} and columns {2tc, 2tc+1} + {0, 16, 32, 48}
+constexpr int CNT = 128;
+template <int OPA, int OPB>
+__device__ __forceinline__ void cg_load(float2 (*sA)[GT], float2 (*sB)[GT], const float2* A, int64_t lda,
+                                        const float2* B, int64_t ldb, int m, int n, int K, int i0, int j0, int k0) {
+  const int tid = threadIdx.x;
+#pragma unroll 2
+  for (int u = 0; u < SK * GT / CNT; ++u) {
+    const int e = tid + CNT * u;
+    int r, kk;
+    if (OPA == OP_T || OPA == OP_C) { kk = e % SK; r = e / SK; } else { r = e % GT; kk = e / GT; }
+    const bool ok = (i0 + r < m) && (k0 + kk < K);
+    const float2* src = A;
+    if (ok) src = (OPA == OP_T || OPA == OP_C) ? A + (k0 + kk) + (int64_t)(i0 + r) * lda : A + (i0 + r) + (int64_t)(k0 + kk) * lda;
+    cp_async8(&sA[kk][r], src, ok);
+    int c;
+    if (OPB == OP_N || OPB == OP_R) { kk = e % SK; c = e / SK; } else { c = e % GT; kk = e / GT; }
+    const bool okb = (j0 + c < n) && (k0 + kk < K);
+    const float2* srcb = B;
+    if (okb) srcb = (OPB == OP_N || OPB == OP_R) ? B + (k0 + kk) + (int64_t)(j0 + c) * ldb : B + (j0 + c) + (int64_t)(k0 + kk) * ldb;
+    cp_async8(&sB[kk][c], srcb, okb);
+  }
+  cp_commit();
+}
+
+template <int OPA, int OPB>
+__device__ __forceinline__ void cg_segment(float (&re)[4][8], float (&im)[4][8], float2 (*sA)[SK][GT], float2 (*sB)[SK][GT],
+                                           const float2* A, int64_t lda, const float2* B, int64_t ldb, int m, int n,
+                                           int K, int i0, int j0, int sb, int se) {
+  constexpr bool CA = (OPA == OP_C || OPA == OP_R), CB = (OPB == OP_C || OPB == OP_R);
+  const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
+  if (sb >= se) return;
+  cg_load<OPA, OPB>(sA[0], sB[0], A, lda, B, ldb, m, n, K, i0, j0, sb * SK);
+  for (int s = sb; s < se; ++s) {
+    const int buf = (s - sb) & 1;
+    if (s + 1 < se) {
+      cg_load<OPA, OPB>(sA[buf ^ 1], sB[buf ^ 1], A, lda, B, ldb, m, n, K, i0, j0, (s + 1) * SK);
+      cp_wait<1>();
+    } else {
+      cp_wait<0>();
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < SK; ++kk) {
+      float ar[4], ai[4], br[8], bi[8];
+      const float4 a0 = *reinterpret_cast<const float4*>(&sA[buf][kk][2 * tr]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&sA[buf][kk][32 + 2 * tr]);
+      ar[0] = a0.x; ai[0] = a0.y; ar[1] = a0.z; ai[1] = a0.w; ar[2] = a1.x; ai[2] = a1.y; ar[3] = a1.z; ai[3] = a1.w;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 b = *reinterpret_cast<const float4*>(&sB[buf][kk][16 * q + 2 * tc]);
+        br[2 * q] = b.x; bi[2 * q] = b.y; br[2 * q + 1] = b.z; bi[2 * q + 1] = b.w;
+      }
+#pragma unroll
+      for (int x = 0; x < 4; ++x) {
+        const float xr = ar[x], xi = CA ? -ai[x] : ai[x];
+#pragma unroll
+        for (int y = 0; y < 8; ++y) {
+          const float yr = br[y], yi = CB ? -bi[y] : bi[y];
+          re[x][y] = fmaf(xr, yr, re[x][y]);
+          re[x][y] = fmaf(-xi, yi, re[x][y]);
+          im[x][y] = fmaf(xr, yi, im[x][y]);
+          im[x][y] = fmaf(xi, yr, im[x][y]);
+        }
+      }
+    }
+    __syncthreads();  // the next stage's copy overwrites this buffer
+  }
+}
+
+template <int OPA1, int OPB1, int OPA2, int OPB2>
+__global__ void __launch_bounds__(CNT) k_cgemm32(ZgemmArgsT<float> g) {
+  __shared__ __align__(16) float2 sA[2][SK][GT];
+  __shared__ __align__(16) float2 sB[2][SK][GT];
+  const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
+  const int i0 = blockIdx.x * GT, j0 = blockIdx.y * GT;
+  const int split = blockIdx.z;
+  float re[4][8], im[4][8];
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 8; ++y) { re[x][y] = 0.f; im[x][y] = 0.f; }
+  {
+    const int steps = ceil_div(g.k1, SK);
+    const int sb = (int)(((int64_t)steps * split) / gridDim.z), se = (int)(((int64_t)steps * (split + 1)) / gridDim.z);
+    cg_segment<OPA1, OPB1>(re, im, sA, sB, g.A1, g.lda1, g.B1, g.ldb1, g.m, g.n, g.k1, i0, j0, sb, se);
+  }
+  if (g.A2 != nullptr) {
+    // s2 = +-1: the second product is added (or subtracted, between two negations)
+    const bool neg = g.s2 < 0.f;
+    if (neg)
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 8; ++y) { re[x][y] = -re[x][y]; im[x][y] = -im[x][y]; }
+    const int steps = ceil_div(g.k2, SK);
+    const int sb = (int)(((int64_t)steps * split) / gridDim.z), se = (int)(((int64_t)steps * (split + 1)) / gridDim.z);
+    cg_segment<OPA2, OPB2>(re, im, sA, sB, g.A2, g.lda2, g.B2, g.ldb2, g.m, g.n, g.k2, i0, j0, sb, se);
+    if (neg)
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 8; ++y) { re[x][y] = -re[x][y]; im[x][y] = -im[x][y]; }
+  }
+  const bool partial = gridDim.z > 1;
+  const float2 al = g.alpha, be = g.beta;
+  const bool use_beta = (be.x != 0.f || be.y != 0.f);
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    const int i = i0 + ((x < 2) ? 2 * tr + x : 32 + 2 * tr + (x - 2));
+    if (i >= g.m) continue;
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+      const int j = j0 + 16 * (y >> 1) + 2 * tc + (y & 1);
+      if (j >= g.n) continue;
+      if (partial) {  // raw partial sums; k_zsplit_reduce applies alpha/beta
+        g.P[(int64_t)split * g.m * g.n + i + (int64_t)j * g.m] = make_float2(re[x][y], im[x][y]);
+        continue;
+      }
+      float2 out = make_float2(al.x * re[x][y] - al.y * im[x][y], al.x * im[x][y] + al.y * re[x][y]);
+      const int64_t o = i + (int64_t)j * g.ldc;
+      if (use_beta) {
+        const float2 c = g.C[o];
+        out.x += be.x * c.x - be.y * c.y;
+        out.y += be.x * c.y + be.y * c.x;
+      }
+      g.C[o] = out;
+    }
+  }
+}
+
+// real grouped, 64 x 64 tile, 64 threads (8 x 8), thread (tr, tc) owns rows
+// {4tr..4tr+3, 32+4tr..} and the same pattern of columns
+constexpr int RNT = 64;
+__global__ void __launch_bounds__(RNT) k_sgemm_grouped(const DgemmDescT<float>* __restrict__ descs, int count) {
+  __shared__ __align__(16) float sA[2][SK][GT];
+  __shared__ __align__(16) float sB[2][SK][GT];
+  const int t = blockIdx.x;
+  int gi = 0;
+  {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (descs[mid].tile0 <= t) lo = mid; else hi = mid - 1;
+    }
+    gi = lo;
+  }
+  const DgemmDescT<float> d = descs[gi];
+  const int local = t - d.tile0;
+  const int mt = (d.m + GT - 1) / GT;
+  const int i0 = (local % mt) * GT, j0 = (local / mt) * GT;
+  const int tid = threadIdx.x;
+  const int tr = tid & 7, tc = tid >> 3;
+  float acc[8][8];
+#pragma unroll
+  for (int x = 0; x < 8; ++x)
+#pragma unroll
+    for (int y = 0; y < 8; ++y) acc[x][y] = 0.f;
+  auto load = [&](int s, int buf) {
+    const int k0 = s * SK;
+#pragma unroll 2
+    for (int u = 0; u < SK * GT / RNT; ++u) {
+      const int e = tid + RNT * u;
+      int r, kk;
+      if (d.ta) { kk = e % SK; r = e / SK; } else { r = e % GT; kk = e / GT; }
+      const bool ok = (i0 + r < d.m) && (k0 + kk < d.k);
+      const float* src = d.A;
+      if (ok) src = d.ta ? d.A + (k0 + kk) + (int64_t)(i0 + r) * d.lda : d.A + (i0 + r) + (int64_t)(k0 + kk) * d.lda;
+      cp_async4(&sA[buf][kk][r], src, ok);
+      int c;
+      if (!d.tb) { kk = e % SK; c = e / SK; } else { c = e % GT; kk = e / GT; }
+      const bool okb = (j0 + c < d.n) && (k0 + kk < d.k);
+      const float* srcb = d.B;
+      if (okb) srcb = d.tb ? d.B + (j0 + c) + (int64_t)(k0 + kk) * d.ldb : d.B + (k0 + kk) + (int64_t)(j0 + c) * d.ldb;
+      cp_async4(&sB[buf][kk][c], srcb, okb);
+    }
+    cp_commit();
+  };
+  const int nst = ceil_div(d.k, SK);
+  if (nst > 0) load(0, 0);
+  for (int s = 0; s < nst; ++s) {
+    const int buf = s & 1;
+    if (s + 1 < nst) { load(s + 1, buf ^ 1); cp_wait<1>(); } else { cp_wait<0>(); }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < SK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&sA[buf][kk][4 * tr]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&sA[buf][kk][32 + 4 * tr]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&sB[buf][kk][4 * tc]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&sB[buf][kk][32 + 4 * tc]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int x = 0; x < 8; ++x)
+#pragma unroll
+        for (int y = 0; y < 8; ++y) acc[x][y] = fmaf(a[x], b[y], acc[x][y]);
+    }
+    __syncthreads();  // the next stage's copy overwrites this buffer
+  }
+#pragma unroll
+  for (int x = 0; x < 8; ++x) {
+    const int i = i0 + ((x < 4) ? 4 * tr + x : 32 + 4 * tr + (x - 4));
+    if (i >= d.m) continue;
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+      const int j = j0 + ((y < 4) ? 4 * tc + y : 32 + 4 * tc + (y - 4));
+      if (j >= d.n) continue;
+      const int64_t o = i + (int64_t)j * d.ldc;
+      float out = d.alpha * acc[x][y];
+      if (d.beta != 0.f) out += d.beta * d.C[o];
+      d.C[o] = out;
+    }
+  }
+}
+
 template <typename R, int OPA1, int OPB1, int OPA2, int OPB2>
 int zgemm_launch(const ZgemmArgsT<R>& g, int batch, cudaStream_t st) {
   if (g.m <= 0 || g.n <= 0) return ZQ_OK;
@@ -186,7 +425,14 @@ int zgemm_launch(const ZgemmArgsT<R>& g, int batch, cudaStream_t st) {
   const int splits = choose_splits(g);
   dim3 grid(ceil_div(g.m, GT), ceil_div(g.n, GT), splits);
   prof_begin(PC_FORMQ_GEMM, st);
-  k_zgemm<R, OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
+  if constexpr (std::is_same<R, float>::value) {
+    if (g.A2 == nullptr || g.s2 == 1.f || g.s2 == -1.f)
+      k_cgemm32<OPA1, OPB1, OPA2, OPB2><<<grid, CNT, 0, st>>>(g);
+    else
+      k_zgemm<R, OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
+  } else {
+    k_zgemm<R, OPA1, OPB1, OPA2, OPB2><<<grid, GNT, 0, st>>>(g);
+  }
   prof_end(PC_FORMQ_GEMM, st);
   ZQ_LAUNCH_CHECK();
   if (splits > 1) {
@@ -293,7 +539,10 @@ __global__ void __launch_bounds__(GNT) k_dgemm_grouped(const DgemmDescT<R>* __re
 template <typename R>
 void grouped_launch(const DgemmDescT<R>* dev_descs, int count, int tiles, cudaStream_t st) {
   if (tiles <= 0 || count <= 0) return;
-  k_dgemm_grouped<R><<<tiles, GNT, 0, st>>>(dev_descs, count);
+  if constexpr (std::is_same<R, float>::value)
+    k_sgemm_grouped<<<tiles, RNT, 0, st>>>(dev_descs, count);
+  else
+    k_dgemm_grouped<R><<<tiles, GNT, 0, st>>>(dev_descs, count);
 }
 template void grouped_launch<double>(const DgemmDescT<double>*, int, int, cudaStream_t);
 template void grouped_launch<float>(const DgemmDescT<float>*, int, int, cudaStream_t);
@@ -313,7 +562,7 @@ int dgemm_grouped(DgemmDescT<R>* host_descs, int count, DgemmDescT<R>* dev_descs
   }
   if (used == 0) return ZQ_OK;
   ZQ_CUDA(cudaMemcpyAsync(dev_descs, host_descs, sizeof(DgemmDescT<R>) * used, cudaMemcpyHostToDevice, st));
-  k_dgemm_grouped<R><<<tiles, GNT, 0, st>>>(dev_descs, used);
+  grouped_launch<R>(dev_descs, used, tiles, st);
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;
 }

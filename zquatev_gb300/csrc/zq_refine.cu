@@ -575,7 +575,15 @@ int refined_solve(RefineArgs& ra) {
   const int64_t ldd = ra.ldd;
   double2* X = ra.dD;  // (U; V) lives in the output's left half
 
+  // ZQ_REFINE_TRACE: per-step history and the stage timeline (events) on stderr
+  const bool trace = getenv("ZQ_REFINE_TRACE") != nullptr;
+  cudaEvent_t tev[9];
+  if (trace)
+    for (auto& e : tev) cudaEventCreate(&e);
+  auto mark = [&](int i, cudaStream_t s2) { if (trace) cudaEventRecord(tev[i], s2); };
+
   // A. FP32 eigendecomposition
+  mark(0, st);
   ZQ_CUDA(cudaMemcpy2DAsync(H0, sizeof(double2) * n2, ra.dD, sizeof(double2) * ldd, sizeof(double2) * n2, n,
                             cudaMemcpyDeviceToDevice, st));
   k_c128_to_c64<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(H0, n2, Mf, n2, n2, n);
@@ -583,18 +591,22 @@ int refined_solve(RefineArgs& ra) {
   TridiagView<float> vf = tridiag_bind<float>(tri_ws, Mf, n, n2, 64, d, e, tau);
   if (int rc = tridiagonalize<float>(vf, ra.nb, st)) return rc;
   if (int rc = phase_reduce(e, n, offd, phi, st)) return rc;
+  mark(1, st);
   float2* XfQ = Mf + (int64_t)n * n2;  // right half of Mf
   // Q Phi (FP32) on the second stream while the divide and conquer runs
   ZQ_CUDA(cudaEventRecord(ra.ev_fork, st));
   ZQ_CUDA(cudaStreamWaitEvent(ra.st2, ra.ev_fork, 0));
   if (int rc = form_q<float>(Mf, n2, n, phi, XfQ, n2, ra.nbq, fq_ws, ra.st2)) return rc;
+  mark(2, ra.st2);
   ZQ_CUDA(cudaEventRecord(ra.ev_join, ra.st2));
   float* Zf = nullptr;  // FP32 divide and conquer: Z in the plan's workspace
   if (int rc = ra.dc->run_single(d, offd, lam, Zf, st)) return rc;
+  mark(3, st);
   ZQ_CUDA(cudaStreamWaitEvent(st, ra.ev_join, 0));
   if (int rc = apply_z<float>(XfQ, n2, Zf, n, n, Mf, n2, ra.fdesc, st)) return rc;
   k_c64_to_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(Mf, n2, X, ldd, n2, n);
   ZQ_LAUNCH_CHECK();
+  mark(4, st);
 
   // B. refinement
   prof_begin(PC_REFINE, st);
@@ -604,7 +616,6 @@ int refined_solve(RefineArgs& ra) {
   ra.last_emax = 1.0;
   const int ne = 1024;
   std::vector<double> hemax(2 * ne);
-  const bool trace = getenv("ZQ_REFINE_TRACE") != nullptr;  // per-step history on stderr
   for (int it = 0; it < ra.max_iter; ++it) {
     // the first correction only has to reach ~1e-8 (the next step squares the
     // error): ZQ_REFINE_SLICES0 slices (default 5 = 35 bits); later steps use 8
@@ -684,12 +695,27 @@ int refined_solve(RefineArgs& ra) {
     k_add_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(P1, n2, X, ldd, n2, n);
     ZQ_LAUNCH_CHECK();
     ra.iters = it + 1;
-    if (trace)
+    if (trace) {
+      mark(5 + (it < 3 ? it : 2), st);
       fprintf(stderr, "zq refine n=%d step %d slices %d emax %.3e coupling %.3e pairs %d clusters %d\n", n, it, sl,
               em, cm, hcount, clusters);
+    }
     if (em <= ra.tol && (ra.mode == 0 || sl == 8)) break;
   }
   prof_end(PC_REFINE, st);
+  if (trace) {
+    mark(8, st);
+    cudaEventSynchronize(tev[8]);
+    float t[9];
+    for (int i = 1; i < 9; ++i) t[i] = -1.f;
+    const int last = 5 + (ra.iters - 1 < 2 ? ra.iters - 1 : 2);
+    for (int i : {1, 2, 3, 4, 5, 6, 7, 8})
+      if (i <= 4 || i <= last || i == 8) cudaEventElapsedTime(&t[i], tev[0], tev[i]);
+    fprintf(stderr, "zq refine timeline ms from start: tridiag+phase %.2f | form_q done (2nd stream) %.2f | "
+            "d&c done %.2f | apply_z done %.2f | step0 %.2f step1 %.2f step2 %.2f | end %.2f\n",
+            t[1], t[2], t[3], t[4], t[5], t[6], t[7], t[8]);
+    for (auto& e : tev) cudaEventDestroy(e);
+  }
   // ascending order
   k_rank<<<ceil_div(n, 128), 128, 0, st>>>(lam, n, rank);
   ZQ_LAUNCH_CHECK();
