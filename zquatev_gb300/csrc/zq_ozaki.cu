@@ -85,13 +85,33 @@ __device__ __forceinline__ void oz_entry(const OzSide& s, bool is_a, int idx, in
 
 // exponent e with 2^e >= max |entry| of row/column idx (e = -1100 for a zero row)
 __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict__ exps) {
+  // The entries of row/column idx over k' are Re x and Im x of each complex x
+  // of the row (times s2 in A's second segment), so the maximum is taken over
+  // max(|Re x|, |Im x|) in one pass with eight loads in flight per lane.
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= count) return;
+  (void)Kp;
   double mx = 0.0;
-  for (int kp = lane; kp < Kp; kp += 32) {
-    double a, b;
-    oz_entry(s, is_a, warp, kp, a, b);
-    mx = fmax(mx, fabs(a));
+  const int nseg = (s.X2 != nullptr && s.K2 > 0) ? 2 : 1;
+  for (int seg = 0; seg < nseg; ++seg) {
+    const double2* X = seg ? s.X2 : s.X1;
+    const int64_t ld = seg ? s.ld2 : s.ld1;
+    const int op = seg ? s.op2 : s.op1;
+    const int K = seg ? s.K2 : s.K1;
+    double m2 = 0.0;
+    for (int k0 = 0; k0 < K; k0 += 32 * 8) {
+      double2 x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = k0 + lane + 32 * u;
+        x[u] = make_double2(0.0, 0.0);
+        if (k < K) x[u] = is_a ? oz_op(X, ld, op, warp, k) : oz_op(X, ld, op, k, warp);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) m2 = fmax(m2, fmax(fabs(x[u].x), fabs(x[u].y)));
+    }
+    // rounding is monotone: max |s2 x| = |s2| max |x| exactly
+    mx = fmax(mx, (is_a && seg) ? fabs(s.s2) * m2 : m2);
   }
   mx = warp_max(mx);
   if (lane == 0) {
@@ -128,24 +148,46 @@ __device__ __forceinline__ unsigned long long oz_fixed(double v, int e, int F, b
 __global__ void k_oz_slice(OzSide s, bool is_a, int count, int count_pad, int Kp, const int* __restrict__ exps,
                            int nsl, __nv_bfloat16* __restrict__ out_re, __nv_bfloat16* __restrict__ out_im,
                            int64_t slice_stride) {
-  const int64_t total = (int64_t)count_pad * Kp;
+  // eight consecutive k' of one row per thread (Kp is a multiple of 64), each
+  // slice written as one 16-byte store
+  const int64_t total8 = (int64_t)count_pad * Kp / 8;
   const int F = OZ_BETA * nsl;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int idx = (int)(t / Kp), kp = (int)(t % Kp);
-    double v[2] = {0.0, 0.0};
-    int e = 0;
-    if (idx < count) {
-      oz_entry(s, is_a, idx, kp, v[0], v[1]);
-      e = exps[idx];
+  for (int64_t t8 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t8 < total8; t8 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = t8 * 8;
+    const int idx = (int)(t / Kp), kp0 = (int)(t % Kp);
+    const bool live = idx < count;
+    const int e = live ? exps[idx] : 0;
+    unsigned long long V0[8], V1[8];
+    unsigned n0 = 0, n1 = 0;  // sign bits
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      double a = 0.0, b = 0.0;
+      if (live) oz_entry(s, is_a, idx, kp0 + u, a, b);
+      bool ng0, ng1;
+      V0[u] = oz_fixed(a, e, F, ng0);
+      V1[u] = oz_fixed(b, e, F, ng1);
+      n0 |= (unsigned)ng0 << u;
+      n1 |= (unsigned)ng1 << u;
     }
-    bool neg[2];
-    const unsigned long long V0 = oz_fixed(v[0], e, F, neg[0]);
-    const unsigned long long V1 = oz_fixed(v[1], e, F, neg[1]);
     for (int q = 0; q < nsl; ++q) {
       const int shift = F - OZ_BETA * (q + 1);
-      const int dr = (int)((V0 >> shift) & 127), di = (int)((V1 >> shift) & 127);
-      out_re[q * slice_stride + t] = __int2bfloat16_rn(neg[0] ? -dr : dr);
-      if (out_im) out_im[q * slice_stride + t] = __int2bfloat16_rn(neg[1] ? -di : di);
+      unsigned pr[4], pi[4];
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        unsigned short lo, hi;
+        int d = (int)((V0[2 * h] >> shift) & 127);
+        lo = __bfloat16_as_ushort(__int2bfloat16_rn(((n0 >> (2 * h)) & 1) ? -d : d));
+        d = (int)((V0[2 * h + 1] >> shift) & 127);
+        hi = __bfloat16_as_ushort(__int2bfloat16_rn(((n0 >> (2 * h + 1)) & 1) ? -d : d));
+        pr[h] = (unsigned)lo | ((unsigned)hi << 16);
+        d = (int)((V1[2 * h] >> shift) & 127);
+        lo = __bfloat16_as_ushort(__int2bfloat16_rn(((n1 >> (2 * h)) & 1) ? -d : d));
+        d = (int)((V1[2 * h + 1] >> shift) & 127);
+        hi = __bfloat16_as_ushort(__int2bfloat16_rn(((n1 >> (2 * h + 1)) & 1) ? -d : d));
+        pi[h] = (unsigned)lo | ((unsigned)hi << 16);
+      }
+      *reinterpret_cast<uint4*>(out_re + q * slice_stride + t) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+      if (out_im) *reinterpret_cast<uint4*>(out_im + q * slice_stride + t) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
     }
   }
 }
@@ -492,13 +534,13 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
     } else {
       k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
       ZQ_LAUNCH_CHECK();
-      k_oz_slice<<<grid(mp * Kp), 256, 0, st>>>(a, true, m, (int)mp, (int)Kp, ea, nsl, As, nullptr, mp * Kp);
+      k_oz_slice<<<grid(mp * Kp / 8), 256, 0, st>>>(a, true, m, (int)mp, (int)Kp, ea, nsl, As, nullptr, mp * Kp);
       ZQ_LAUNCH_CHECK();
     }
   }
   k_oz_exp<<<ceil_div(n * 32, 256), 256, 0, st>>>(b, false, n, (int)Kp, eb);
   ZQ_LAUNCH_CHECK();
-  k_oz_slice<<<grid(np * Kp), 256, 0, st>>>(b, false, n, (int)np, (int)Kp, eb, nsl, Brs, Bis, np * Kp);
+  k_oz_slice<<<grid(np * Kp / 8), 256, 0, st>>>(b, false, n, (int)np, (int)Kp, eb, nsl, Brs, Bis, np * Kp);
   ZQ_LAUNCH_CHECK();
   OzGemmArgs og{};
   og.A = As; og.Bre = Brs; og.Bim = Bis; og.sa = mp * Kp; og.sb = np * Kp;
