@@ -466,6 +466,8 @@ int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cu
   ra.pair_eps = 1e-4;  // |E| <= 1e-4 from the formula: two more steps reach 1e-7
   ra.slices0 = 5;
   if (const char* s = getenv("ZQ_REFINE_SLICES0")) { const int v = atoi(s); if (v >= 3 && v <= 8) ra.slices0 = v; }
+  ra.slices_res = 4;
+  if (const char* s = getenv("ZQ_REFINE_RSLICES")) { const int v = atoi(s); if (v >= 2 && v <= 8) ra.slices_res = v; }
   if (const char* s = getenv("ZQ_REFINE_MAXIT")) ra.max_iter = atoi(s);
   if (const char* s = getenv("ZQ_REFINE_EPS")) { const double v = atof(s); if (v > 0.0 && v < 0.5) ra.pair_eps = v; }
   ra.st = c->st;

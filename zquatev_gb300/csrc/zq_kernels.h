@@ -153,6 +153,7 @@ struct RefineArgs {
   double cluster_tol;          // accepted in-cluster coupling (relative to max |lambda|)
   double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap|
   int slices0;                 // Ozaki slices of the first step's products
+  int slices_res;              // Ozaki slices of the products with the residual R = HX - X Lambda
   cudaStream_t st;
   cudaStream_t st2;            // second stream: Q formation overlaps the tridiagonal solve
   cudaEvent_t ev_fork, ev_join;
@@ -169,6 +170,7 @@ struct OzOpts {
   int slices;      // bf16 slices per operand (7 bits each), 2..8
   int structured;  // 0 general; +1 Hermitian / -1 antisymmetric square output (lower tiles computed)
   int reuse_a;     // 1: the A operand is the same as in the previous call (slices kept)
+  int nofill;      // structured: leave the upper triangle to the caller (who fills it with structured_fill)
 };
 int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st,
                 const OzOpts& opt);

@@ -592,7 +592,7 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
     prof_end(PC_OZAKI, st);
     ZQ_LAUNCH_CHECK();
   }
-  if (opt.structured != 0) {
+  if (opt.structured != 0 && !opt.nofill) {
     k_oz_symfill<<<grid((int64_t)m * n), 256, 0, st>>>(g.C, g.ldc, m, opt.structured);
     ZQ_LAUNCH_CHECK();
   }

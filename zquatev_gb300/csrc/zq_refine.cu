@@ -70,14 +70,38 @@ __global__ void k_add_c128(const double2* __restrict__ y, int64_t ldy, double2* 
 // H X from P1 = [A;B] U and P2 = [A;B] conj(V) (both 2n x n, ld):
 //   (HX)_top = P1_top - conj(P2_bot),  (HX)_bot = P1_bot + conj(P2_top)
 __global__ void k_hx_combine(const double2* __restrict__ P1, const double2* __restrict__ P2, int64_t ldp, int n,
-                             double2* __restrict__ HX, int64_t ldh) {
+                             double2* __restrict__ HX, int64_t ldh, const double2* __restrict__ X, int64_t ldx,
+                             const double* __restrict__ lam) {
+  // HX (left half) from P1 = [A;B] U and P2 = [A;B] conj(V); with lam given,
+  // the residual R = HX - X diag(lam) instead
   const int64_t total = (int64_t)n * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int r = (int)(t % n), c = (int)(t / n);
     const double2 p1t = P1[r + (int64_t)c * ldp], p1b = P1[n + r + (int64_t)c * ldp];
     const double2 p2t = P2[r + (int64_t)c * ldp], p2b = P2[n + r + (int64_t)c * ldp];
-    HX[r + (int64_t)c * ldh] = make_double2(p1t.x - p2b.x, p1t.y + p2b.y);
-    HX[n + r + (int64_t)c * ldh] = make_double2(p1b.x + p2t.x, p1b.y - p2t.y);
+    double2 top = make_double2(p1t.x - p2b.x, p1t.y + p2b.y);
+    double2 bot = make_double2(p1b.x + p2t.x, p1b.y - p2t.y);
+    if (lam) {
+      const double l = lam[c];
+      const double2 xt = X[r + (int64_t)c * ldx], xb = X[n + r + (int64_t)c * ldx];
+      top.x -= xt.x * l; top.y -= xt.y * l;
+      bot.x -= xb.x * l; bot.y -= xb.y * l;
+    }
+    HX[r + (int64_t)c * ldh] = top;
+    HX[n + r + (int64_t)c * ldh] = bot;
+  }
+}
+
+// S += G diag(lam) (n x n, ld n): S = X^H R + G Lambda (and the same for the
+// antisymmetric pair) recovers X^H H X from the residual products
+__global__ void k_add_glam(double2* __restrict__ S, const double2* __restrict__ G, int n, const double* __restrict__ lam) {
+  const int64_t total = (int64_t)n * n;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const double l = lam[t / n];
+    const double2 g = G[t];
+    double2 v = S[t];
+    v.x += g.x * l; v.y += g.y * l;
+    S[t] = v;
   }
 }
 
@@ -405,7 +429,7 @@ size_t refine_workspace_bytes(int n, int nbq) {
   b += sizeof(double2) * 2 * nn;        // Et, Eb
   b += tridiag_workspace_bytes<float>(n, 64);
   b += form_q_workspace_bytes(n, nbq);  // sized for double2, enough for float2
-  b += sizeof(double) * (45 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64);
+  b += sizeof(double) * (46 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64);
   b += sizeof(int) * (size_t)n;
   b += 64 * 256;
   return b;
@@ -415,15 +439,19 @@ size_t refine_workspace_bytes(int n, int nbq) {
 // Structured outputs (G1, S1 Hermitian; G2, S2 antisymmetric) are made exactly
 // structured from their lower triangles, so that the symmetric part of E is R
 // exactly and the orthogonality of the update does not depend on eigenvalue gaps.
+// structured: 0 general; +-1 Hermitian / antisymmetric square output (lower
+// tiles computed, upper filled); +-2 the lower triangle only, the caller fills
 static int zgemm_acc(int mode, int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ows, size_t ows_bytes,
                      cudaStream_t st, int slices, int structured, int reuse_a) {
+  const int sym = structured > 0 ? 1 : (structured < 0 ? -1 : 0);
+  const bool fill = structured == 1 || structured == -1;
   if (mode == 1) {
     OzOpts o{};
-    o.slices = slices; o.structured = structured; o.reuse_a = reuse_a;
+    o.slices = slices; o.structured = sym; o.reuse_a = reuse_a; o.nofill = fill ? 0 : 1;
     return zgemm_ozaki(opa1, opb1, opa2, opb2, g, ows, ows_bytes, st, o);
   }
   if (int rc = zgemm<double>(opa1, opb1, opa2, opb2, g, 1, st)) return rc;
-  if (structured != 0) return structured_fill(g.C, g.ldc, g.m, structured, st);
+  if (fill) return structured_fill(g.C, g.ldc, g.m, sym, st);
   return ZQ_OK;
 }
 
@@ -558,7 +586,7 @@ int refined_solve(RefineArgs& ra) {
   double2* Eb = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
   void* tri_ws = take(tridiag_workspace_bytes<float>(n, 64));
   void* fq_ws = take(form_q_workspace_bytes(n, ra.nbq));
-  double* sm = reinterpret_cast<double*>(take(sizeof(double) * (45 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64)));
+  double* sm = reinterpret_cast<double*>(take(sizeof(double) * (46 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64)));
   int* rank = reinterpret_cast<int*>(take(sizeof(int) * (size_t)n));
   double* d = sm; sm += n;
   double* e = sm; sm += 4 * (size_t)n;
@@ -567,6 +595,7 @@ int refined_solve(RefineArgs& ra) {
   double* phi = sm; sm += 4 * (size_t)n;
   double* lam = sm; sm += n;
   double* lam2 = sm; sm += n;
+  double* lamr = sm; sm += n;   // the diagonal of the current step's residual R = HX - X diag(lamr)
   double* part = sm; sm += 3 * 8192;
   double* emax = sm; sm += 2048;
   int* pair_count = reinterpret_cast<int*>(sm); sm += 8;
@@ -626,6 +655,9 @@ int refined_solve(RefineArgs& ra) {
     // 3 slices (21 bits) first, 4 (28 bits) after keep its error below what
     // the next step removes / below 1e-14
     const int sl_upd = (it == 0) ? 3 : 4;
+    // the residual products: |R| <= ~1e-4 ||H|| in the first step, ~1e-8 after,
+    // so 4 slices (28 bits) leave their error below what each step needs
+    const int ss_slices = ra.slices_res;
     double2* U = X;
     double2* V = X + n;
     ZgemmArgs g{};
@@ -638,23 +670,35 @@ int refined_solve(RefineArgs& ra) {
     if (int rc = zgemm_acc(ra.mode, OP_N, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 0, 0)) return rc;
     g.B1 = V; g.C = P2;
     if (int rc = zgemm_acc(ra.mode, OP_N, OP_R, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 0, 1)) return rc;
-    k_hx_combine<<<grid_for((int64_t)nn), 256, 0, st>>>(P1, P2, n2, n, HX, n2);
+    // R = HX - X diag(lamr), lamr the current eigenvalue estimates (the
+    // divide-and-conquer values, then the previous step's Rayleigh quotients).
+    // S = X^H H X = X^H R + G diag(lamr) for any diagonal lamr; with R small
+    // (~ the eigenvector error times ||H||) the products with R need only
+    // ss_slices, while G keeps sl.
+    ZQ_CUDA(cudaMemcpyAsync(lamr, lam, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    k_hx_combine<<<grid_for((int64_t)nn), 256, 0, st>>>(P1, P2, n2, n, HX, n2, X, ldd, lamr);
     ZQ_LAUNCH_CHECK();
-    // G1 = X^H X ; S1 = X^H HX
+    // G1 = X^H X ; S1 = X^H R + G1 Lambda
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n2; g.A1 = X; g.lda1 = ldd; g.B1 = X; g.ldb1 = ldd;
     g.alpha = one; g.beta = zero; g.C = G1; g.ldc = n;
     if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 0)) return rc;
     g.B1 = HX; g.ldb1 = n2; g.C = S1;
-    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, sl, 1, 1)) return rc;
-    // G2 = U^T V - V^T U ; S2 = U^T HX_bot - V^T HX_top
+    if (int rc = zgemm_acc(ra.mode, OP_C, OP_N, OP_N, OP_N, g, ra.ows, ra.ows_bytes, st, ss_slices, 2, 1)) return rc;
+    // G2 = U^T V - V^T U ; S2 = U^T R_bot - V^T R_top + G2 Lambda
     g = ZgemmArgs{};
     g.m = n; g.n = n; g.k1 = n; g.k2 = n;
     g.A1 = U; g.lda1 = ldd; g.B1 = V; g.ldb1 = ldd; g.A2 = V; g.lda2 = ldd; g.B2 = U; g.ldb2 = ldd; g.s2 = -1.0;
     g.alpha = one; g.beta = zero; g.C = G2; g.ldc = n;
     if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 0)) return rc;
     g.B1 = HX + n; g.ldb1 = n2; g.B2 = HX; g.ldb2 = n2; g.C = S2;
-    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, sl, -1, 1)) return rc;
+    if (int rc = zgemm_acc(ra.mode, OP_T, OP_N, OP_T, OP_N, g, ra.ows, ra.ows_bytes, st, ss_slices, -2, 1)) return rc;
+    k_add_glam<<<grid_for((int64_t)nn), 256, 0, st>>>(S1, G1, n, lamr);
+    ZQ_LAUNCH_CHECK();
+    k_add_glam<<<grid_for((int64_t)nn), 256, 0, st>>>(S2, G2, n, lamr);
+    ZQ_LAUNCH_CHECK();
+    if (int rc = structured_fill(S1, n, n, 1, st)) return rc;
+    if (int rc = structured_fill(S2, n, n, -1, st)) return rc;
     // Rayleigh quotients, coupling norms, E; pairs that fail the first-order
     // test are grouped into clusters, rotated (Rayleigh-Ritz on the current
     // basis, S and G carried along), and E is rebuilt in the rotated basis
