@@ -45,6 +45,7 @@ constexpr int UM_CH = 512;           // K terms per exact FP32 accumulation (512
 constexpr int UM_SUPER = 64 * 1024;  // K terms per int32 partial (65536 * 127^2 < 2^31)
 constexpr int UM_BETA = 7;
 constexpr int UM_THREADS = 320;
+constexpr int UM_GROUP = 16;          // row tiles per group of the full-tile launch order
 constexpr uint32_t UM_A_BYTES = UM_BM * UM_BK * 2;       // 16 KB
 constexpr uint32_t UM_BH_BYTES = UM_BN * UM_BK * 2;      // 16 KB (Bre or Bim half)
 constexpr uint32_t UM_STAGE_BYTES = UM_A_BYTES + 2 * UM_BH_BYTES;
@@ -179,10 +180,18 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   const uint32_t tmem = s_tmem;
   volatile int* abort = &s_abort;
 
-  int bi = blockIdx.x, bj = blockIdx.y;
+  int bi, bj;
   if (g.lower) {
-    const int t = blockIdx.x;
-    tri_tile(t, bi, bj);
+    tri_tile((int)blockIdx.x, bi, bj);
+  } else {
+    // grouped order: runs of UM_GROUP row tiles sweep the column tiles
+    // together, so the CTAs resident at one time share their A and B slices
+    // in L2 (a wave covers ~16 x 10 tiles instead of all row tiles x 2)
+    const int tm = g.mp / UM_BM, tn = g.np / UM_BN;  // the host's grid is tm * tn
+    const int t = (int)blockIdx.x, per = UM_GROUP * tn, grp = t / per, first = grp * UM_GROUP;
+    const int gm = (tm - first) < UM_GROUP ? (tm - first) : UM_GROUP;
+    bi = first + (t % per) % gm;
+    bj = (t % per) / gm;
   }
   const int i0 = bi * UM_BM, j0 = bj * UM_BN;
   const int Kp = g.Kp;
@@ -378,7 +387,7 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
   a.mp = mp; a.np = np; a.Kp = Kp; a.m = m; a.n = n; a.nsl = nsl; a.lower = lower;
   a.ea = ea; a.eb = eb; a.C = C; a.ldc = ldc; a.err = err;
   const int tm = mp / UM_BM, tn = np / UM_BN;
-  const dim3 grid = lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)tm, (unsigned)tn);
+  const dim3 grid = lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)(tm * tn), 1);
   ZQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   k_oz_umma<<<grid, UM_THREADS, UM_SMEM, st>>>(ta, tbr, tbi, a);
   ZQ_LAUNCH_CHECK();
