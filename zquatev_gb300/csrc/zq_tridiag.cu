@@ -433,8 +433,10 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int p, int j, in
     const int gr = rbase + r, gc = cbase + c;
     ta[u] = czero<Z>(); tb[u] = czero<Z>();
     if (gr < n && gc < n && (!diag || r >= c)) {
-      ta[u] = A[gr + (int64_t)gc * ld];
-      tb[u] = B[gr + (int64_t)gc * ld];
+      // streaming loads (evict first): the trailing matrix passes through L2
+      // once per column, the tile partials written below are read next
+      ta[u] = __ldcs(A + gr + (int64_t)gc * ld);
+      tb[u] = __ldcs(B + gr + (int64_t)gc * ld);
     }
   }
   const int ws = tid >> 5, wq = tid & (HT - 1);
@@ -477,16 +479,24 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int p, int j, in
       cfma(p2, m1, sx[1][c + 1]); cfma(p3, m1, sz[1][c + 1]);
     }
   } else if (role == 2) {
-    for (int r = diag ? q + 1 : 0; r < HT; ++r) {
-      const Z m = sA[r + q * HLD];
-      if (r & 1) { cfmac(p2, m, sx[0][r]); cfmac(p3, m, sz[0][r]); }
-      else { cfmac(p0, m, sx[0][r]); cfmac(p1, m, sz[0][r]); }
+    // column q: rows above q are zero in a diagonal tile; the diagonal itself
+    // belongs to the row products
+#pragma unroll
+    for (int r = 0; r < HT; r += 2) {
+      Z m0 = sA[r + q * HLD], m1 = sA[r + 1 + q * HLD];
+      if (diag && r == q) m0 = czero<Z>();
+      if (diag && r + 1 == q) m1 = czero<Z>();
+      cfmac(p0, m0, sx[0][r]); cfmac(p1, m0, sz[0][r]);
+      cfmac(p2, m1, sx[0][r + 1]); cfmac(p3, m1, sz[0][r + 1]);
     }
   } else {
-    for (int r = diag ? q + 1 : 0; r < HT; ++r) {
-      const Z m = sB[r + q * HLD];
-      if (r & 1) { cfma(p2, m, sx[0][r]); cfma(p3, m, sz[0][r]); }
-      else { cfma(p0, m, sx[0][r]); cfma(p1, m, sz[0][r]); }
+#pragma unroll
+    for (int r = 0; r < HT; r += 2) {
+      Z m0 = sB[r + q * HLD], m1 = sB[r + 1 + q * HLD];
+      if (diag && r == q) m0 = czero<Z>();
+      if (diag && r + 1 == q) m1 = czero<Z>();
+      cfma(p0, m0, sx[0][r]); cfma(p1, m0, sz[0][r]);
+      cfma(p2, m1, sx[0][r + 1]); cfma(p3, m1, sz[0][r + 1]);
     }
     p0 = cneg(p0); p1 = cneg(p1); p2 = cneg(p2); p3 = cneg(p3);
   }
