@@ -361,23 +361,34 @@ __global__ void __launch_bounds__(RNT) k_sgemm_grouped(const DgemmDescT<float>* 
   for (int x = 0; x < 8; ++x)
 #pragma unroll
     for (int y = 0; y < 8; ++y) acc[x][y] = 0.f;
+  // Copy u of this thread (u < 16): with e = tid + 64 u the element is
+  // (row tid, k u) of a row-fast operand or (row tid/16 + 4u, k tid%16) of a
+  // k-fast one, so address, bounds and shared offset are per-thread constants
+  // plus u times a step, computed once per tile.
+  const int lo = tid % SK, hi = tid / SK;
+  // A: rows i0.., k; ta: k-fast
+  const int a_r0 = d.ta ? hi : tid, a_rs = d.ta ? 4 : 0, a_k0 = d.ta ? lo : 0, a_ks = d.ta ? 0 : 1;
+  const float* a_base = d.A + (d.ta ? (a_k0 + (int64_t)(i0 + a_r0) * d.lda) : ((i0 + a_r0) + (int64_t)a_k0 * d.lda));
+  const int64_t a_kstep = d.ta ? 1 : d.lda, a_ustep = d.ta ? 4 * d.lda : d.lda;
+  // B: columns j0.., k; !tb: k-fast
+  const int b_c0 = d.tb ? tid : hi, b_cs = d.tb ? 0 : 4, b_k0 = d.tb ? 0 : lo, b_ks = d.tb ? 1 : 0;
+  const float* b_base = d.B + (d.tb ? ((j0 + b_c0) + (int64_t)b_k0 * d.ldb) : (b_k0 + (int64_t)(j0 + b_c0) * d.ldb));
+  const int64_t b_kstep = d.tb ? d.ldb : 1, b_ustep = d.tb ? d.ldb : 4 * d.ldb;
   auto load = [&](int s, int buf) {
     const int k0 = s * SK;
+    const float* pa = a_base + (int64_t)k0 * a_kstep;
+    const float* pb = b_base + (int64_t)k0 * b_kstep;
+    int ar = a_r0, ak = a_k0 + k0, bc = b_c0, bk = b_k0 + k0;
+    float* da = &sA[buf][a_k0][a_r0];
+    float* db = &sB[buf][b_k0][b_c0];
 #pragma unroll 2
     for (int u = 0; u < SK * GT / RNT; ++u) {
-      const int e = tid + RNT * u;
-      int r, kk;
-      if (d.ta) { kk = e % SK; r = e / SK; } else { r = e % GT; kk = e / GT; }
-      const bool ok = (i0 + r < d.m) && (k0 + kk < d.k);
-      const float* src = d.A;
-      if (ok) src = d.ta ? d.A + (k0 + kk) + (int64_t)(i0 + r) * d.lda : d.A + (i0 + r) + (int64_t)(k0 + kk) * d.lda;
-      cp_async4(&sA[buf][kk][r], src, ok);
-      int c;
-      if (!d.tb) { kk = e % SK; c = e / SK; } else { c = e % GT; kk = e / GT; }
-      const bool okb = (j0 + c < d.n) && (k0 + kk < d.k);
-      const float* srcb = d.B;
-      if (okb) srcb = d.tb ? d.B + (j0 + c) + (int64_t)(k0 + kk) * d.ldb : d.B + (k0 + kk) + (int64_t)(j0 + c) * d.ldb;
-      cp_async4(&sB[buf][kk][c], srcb, okb);
+      const bool ok = (i0 + ar < d.m) && (ak < d.k);
+      cp_async4(da, ok ? pa : d.A, ok);
+      const bool okb = (j0 + bc < d.n) && (bk < d.k);
+      cp_async4(db, okb ? pb : d.B, okb);
+      pa += a_ustep; ar += a_rs; ak += a_ks; da += a_ks * GT + a_rs;
+      pb += b_ustep; bc += b_cs; bk += b_ks; db += b_ks * GT + b_cs;
     }
     cp_commit();
   };

@@ -120,22 +120,44 @@ __device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
   }
   v.scal[4] = f;
   for (int q = 0; q < 4; ++q) v.scal[5 + q] = m[q] * f;
+  // the same head rounded to R once (scal[12..15] as floats): the FP32 kernels
+  // then read it without double-precision conversions
+  float* hf = reinterpret_cast<float*>(v.scal + 12);
+  hf[0] = (float)f;
+  for (int q = 0; q < 4; ++q) hf[1 + q] = (float)(m[q] * f);
+  hf[5] = (f > 0.0) ? 1.f : 0.f;
   for (int q = 0; q < 4; ++q) v.e[4 * j + q] = ee[q];
   v.tau[j] = (f > 0.0) ? 1.0 : 0.0;
 }
 
-// w at row r of column j from x (= the stored column before hreduce writes w):
-// the head row j+1 takes f m, the others f x; no reflector (f = 0) gives 0.
+// the reflector head in the kernel's precision: f, f m (4 reals), and whether
+// a reflector exists (f > 0)
 template <typename R>
-__device__ __forceinline__ void w_from_x(const double* h, int r, int j, cplx<R>& wa, cplx<R>& wb) {
-  const double f = h[0];
-  if (!(f > 0.0)) { wa = czero<cplx<R>>(); wb = czero<cplx<R>>(); return; }
+struct WHead {
+  R f, m[4];
+  bool live;
+};
+__device__ __forceinline__ void load_head(const TridiagView<float>& v, WHead<float>& h) {
+  const float* hf = reinterpret_cast<const float*>(v.scal + 12);
+  h.f = hf[0]; h.m[0] = hf[1]; h.m[1] = hf[2]; h.m[2] = hf[3]; h.m[3] = hf[4];
+  h.live = hf[5] != 0.f;
+}
+__device__ __forceinline__ void load_head(const TridiagView<double>& v, WHead<double>& h) {
+  h.f = v.scal[4]; h.m[0] = v.scal[5]; h.m[1] = v.scal[6]; h.m[2] = v.scal[7]; h.m[3] = v.scal[8];
+  h.live = h.f > 0.0;
+}
+
+// w at row r of column j from x (= the stored column before hreduce writes w):
+// the head row j+1 takes f m, the others f x; no reflector gives 0.
+template <typename R>
+__device__ __forceinline__ void w_from_x(const WHead<R>& h, int r, int j, cplx<R>& wa, cplx<R>& wb) {
+  if (!h.live) { wa = czero<cplx<R>>(); wb = czero<cplx<R>>(); return; }
   if (r == j + 1) {
-    wa = mk((R)h[1], (R)h[2]);
-    wb = mk((R)h[3], (R)h[4]);
+    wa = mk(h.m[0], h.m[1]);
+    wb = mk(h.m[2], h.m[3]);
   } else {
-    wa = cscale(wa, (R)f);
-    wb = cscale(wb, (R)f);
+    wa = cscale(wa, h.f);
+    wb = cscale(wb, h.f);
   }
 }
 
@@ -298,11 +320,10 @@ __device__ void panel_dots(const TridiagView<R>& v, int p, int j, int k, int b, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gr = j + 1 + b * DR + warp * 32 + lane;
   const bool live = gr < n;
-  double h[5];
+  WHead<R> h;
   Z xa = czero<Z>(), xb = czero<Z>();
   if (live) {
-#pragma unroll
-    for (int u = 0; u < 5; ++u) h[u] = v.scal[4 + u];
+    load_head(v, h);
     xa = A[gr + (int64_t)j * ld];
     xb = B[gr + (int64_t)j * ld];
   }
@@ -443,10 +464,9 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int p, int j, in
   const int wg = (ws == 0 ? rbase : cbase) + wq;
   const bool wrow = tid < 2 * HT && wg < n;
   Z x = czero<Z>(), z = czero<Z>();
-  double h[5];
+  WHead<R> h;
   if (wrow) {
-#pragma unroll
-    for (int u = 0; u < 5; ++u) h[u] = v.scal[4 + u];
+    load_head(v, h);
     x = A[wg + (int64_t)j * ld];
     z = B[wg + (int64_t)j * ld];
   }
@@ -548,11 +568,10 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
   __shared__ Z s_red[HNG][HRB][2];
   __shared__ double s_redd[NT / 32];
   // this row's x and the reflector head (w = f x is written in place at the end)
-  double h[5];
+  WHead<R> h;
   Z xa = czero<Z>(), xb = czero<Z>();
   if (grp == 0 && r < n) {
-#pragma unroll
-    for (int u = 0; u < 5; ++u) h[u] = v.scal[4 + u];
+    load_head(v, h);
     xa = A[r + (int64_t)j * ld];
     xb = B[r + (int64_t)j * ld];
   }
