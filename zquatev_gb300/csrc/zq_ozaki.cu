@@ -199,31 +199,52 @@ __global__ void k_oz_exp_init(int* __restrict__ exps, int count) {
   if (i < count) exps[i] = -1100;
 }
 // block (32, 8): 32 rows x 256 K terms; the per-row maximum exponent via atomicMax (order-free)
-__global__ void k_oz_exp_cm(OzSide s, int count, int Kp, int* __restrict__ exps) {
-  __shared__ int s_e[8][32];
+__global__ void k_oz_exp_cm(OzSide s, int count, int Kc, int* __restrict__ exps) {
+  // rows of a column-major op(A) (OP_N / OP_R): 32 rows x 256 complex columns
+  // per CTA, rows on the lanes (coalesced); the maximum of max(|Re x|, |Im x|)
+  // (times |s2| in the second segment) over each complex column once, eight
+  // loads in flight per thread; its exponent equals the largest digit
+  // exponent of the row's entries (frexp is monotone in |a|)
+  __shared__ double s_m[8][32];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int row = blockIdx.x * 32 + tx;
   const int kb = blockIdx.y * 256;
-  int e = -1100;
+  double mx = 0.0;
   if (row < count) {
-    for (int q = ty; q < 256; q += 8) {
-      const int kp = kb + q;
-      if (kp >= Kp) break;
-      double a, b;
-      oz_entry(s, true, row, kp, a, b);
-      if (a != 0.0) {
-        int ex;
-        frexp(a, &ex);  // 2^ex > |a|
-        e = ex > e ? ex : e;
+    for (int q0 = ty; q0 < 256; q0 += 8 * 8) {
+      double2 x[8];
+      double sc[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = kb + q0 + 8 * u;
+        x[u] = make_double2(0.0, 0.0);
+        sc[u] = 1.0;
+        if (q0 + 8 * u < 256 && k < Kc) {
+          if (k < s.K1) {
+            x[u] = oz_op(s.X1, s.ld1, s.op1, row, k);
+          } else {
+            x[u] = oz_op(s.X2, s.ld2, s.op2, row, k - s.K1);
+            sc[u] = fabs(s.s2);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const double m = fmax(fabs(x[u].x), fabs(x[u].y));
+        mx = fmax(mx, sc[u] == 1.0 ? m : sc[u] * m);
       }
     }
   }
-  s_e[ty][tx] = e;
+  s_m[ty][tx] = mx;
   __syncthreads();
   if (ty == 0 && row < count) {
-    int m = s_e[0][tx];
-    for (int r = 1; r < 8; ++r) m = s_e[r][tx] > m ? s_e[r][tx] : m;
-    if (m > -1100) atomicMax(exps + row, m);
+    double m = s_m[0][tx];
+    for (int r = 1; r < 8; ++r) m = fmax(m, s_m[r][tx]);
+    if (m > 0.0) {
+      int ex;
+      frexp(m, &ex);  // 2^ex > m
+      atomicMax(exps + row, ex);
+    }
   }
 }
 // block (32, 8): a 32-row x 32-K tile, digits staged in shared memory, stored along K
@@ -525,8 +546,8 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
       // rows of op(A) are strided: column-wise passes (coalesced reads)
       k_oz_exp_init<<<ceil_div(m, 256), 256, 0, st>>>(ea, m);
       ZQ_LAUNCH_CHECK();
-      k_oz_exp_cm<<<dim3((unsigned)ceil_div(m, 32), (unsigned)ceil_div((int)Kp, 256)), dim3(32, 8), 0, st>>>(a, m, (int)Kp,
-                                                                                                             ea);
+      const int Kc = g.k1 + (two ? g.k2 : 0);  // complex columns of op(A)
+      k_oz_exp_cm<<<dim3((unsigned)ceil_div(m, 32), (unsigned)ceil_div(Kc, 256)), dim3(32, 8), 0, st>>>(a, m, Kc, ea);
       ZQ_LAUNCH_CHECK();
       k_oz_slice_cm<<<dim3((unsigned)(mp / 32), (unsigned)ceil_div((int)Kp, 32)), dim3(32, 8), 0, st>>>(a, m, (int)Kp, ea,
                                                                                                         nsl, As, mp * Kp);
