@@ -23,10 +23,10 @@ struct TridiagView {
   cplx<R>* gb;
   cplx<R>* hpart;  // hemv tile partials: hblk x hblk x 64 x 4
   int hblk;
-  cplx<R>* dpart;  // dot partials: hblk x nbmax x 4
-  cplx<R>* dots;   // 4 * nbmax
+  cplx<R>* dpart;  // panel dot partials, one set per 128 rows: hblk x nbmax x 4 (room for 4x that)
+  cplx<R>* dots;   // the summed panel dot products: 4 * nbmax
   double* npart;   // norm partials: 2 * hblk
-  double* cpart;   // c partials: hblk
+  double* cpart;   // c partials, one per hreduce CTA: ceil(n / 8) + 1
   double* scal;    // per-column scalars (16): [0..3] x_1 of the column, [4] f, [5..8] f m (reflector head)
   unsigned* counter;  // colupd CTAs finished for the current column (the last one forms the reflector)
   double* d;       // diagonal (n)
