@@ -9,6 +9,13 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+def bench_kind() -> str:
+    sys.path.insert(0, ROOT)
+    import bench
+
+    return bench.cpu_kind()
+
+
 def test_reference_arm_json_line():
     out = subprocess.run(
         [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "2", "--warmup", "1",
@@ -25,7 +32,7 @@ def test_reference_arm_json_line():
     assert d["steps"] == 2 and d["warmup"] == 1 and d["n_gpus"] == 1
     assert d["higher_is_better"] is False and d["unit"] == "ms" and d["value"] > 0
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["kind"] == bench_kind() and d["cpu_baseline"]["cores"] >= 1
 
     sys.path.insert(0, ROOT)
     import bench
