@@ -39,3 +39,19 @@ def test_reference_arm_json_line():
 
     assert d["config"] == bench.workload_config(8192, 1)
     assert d["metric"] == bench.METRIC
+
+
+def test_cpu_baseline_falls_back_to_the_port(monkeypatch):
+    """Where the compiled reference does not exist or does not load (the GPU
+    host has neither its sources nor x86 binaries), the baseline is the port
+    on an n2 = 1024 sample."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import ref
+
+    monkeypatch.setattr(ref, "available", lambda: False)
+    assert bench.cpu_kind() == "port"
+    assert bench.cpu_sample_n2(0) == 1024
+    assert bench.cpu_sample_n2(512) == 512
+    ms, raw = bench.cpu_sample(64, 128, 1)
+    assert raw > 0 and abs(ms - raw * 1e3 * 8) < 1e-6 * ms
