@@ -171,6 +171,49 @@ extern "C" __global__ void dmma_peak(double* out, int iters) {
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = c0 + c1 + c2 + c3 + c4 + c5 + c6 + c7;
 }
+// the larger f64 shapes: four independent m16n8kK chains per warp
+extern "C" __global__ void dmma_k4(double* out, int iters) {
+  const double a = 1.0 + threadIdx.x * 1e-3, b = 0.5;
+  double c[4][4] = {};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      asm volatile("mma.sync.aligned.m16n8k4.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+                   : "+d"(c[q][0]), "+d"(c[q][1]), "+d"(c[q][2]), "+d"(c[q][3]) : "d"(a), "d"(a), "d"(b));
+  }
+  double s = 0;
+  for (int q = 0; q < 4; ++q) s += c[q][0] + c[q][1] + c[q][2] + c[q][3];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+extern "C" __global__ void dmma_k8(double* out, int iters) {
+  const double a = 1.0 + threadIdx.x * 1e-3, b = 0.5;
+  double c[4][4] = {};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      asm volatile("mma.sync.aligned.m16n8k8.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+                   : "+d"(c[q][0]), "+d"(c[q][1]), "+d"(c[q][2]), "+d"(c[q][3])
+                   : "d"(a), "d"(a), "d"(a), "d"(a), "d"(b), "d"(b));
+  }
+  double s = 0;
+  for (int q = 0; q < 4; ++q) s += c[q][0] + c[q][1] + c[q][2] + c[q][3];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+extern "C" __global__ void dmma_k16(double* out, int iters) {
+  const double a = 1.0 + threadIdx.x * 1e-3, b = 0.5;
+  double c[4][4] = {};
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      asm volatile("mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7,%8,%9,%10,%11}, "
+                   "{%12,%13,%14,%15}, {%0,%1,%2,%3};"
+                   : "+d"(c[q][0]), "+d"(c[q][1]), "+d"(c[q][2]), "+d"(c[q][3])
+                   : "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(b), "d"(b), "d"(b), "d"(b));
+  }
+  double s = 0;
+  for (int q = 0; q < 4; ++q) s += c[q][0] + c[q][1] + c[q][2] + c[q][3];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 """
 
 
@@ -194,24 +237,34 @@ def fp64_peak_tflops() -> float:
     return best
 
 
-def dmma_peak_tflops() -> float:
-    """FP64 tensor-core (DMMA m8n8k4) throughput of this GPU (TFLOP/s), CUDA events."""
+# flops of one warp-wide mma.sync of each f64 shape, and per-iteration MMAs
+DMMA_SHAPES = {"m8n8k4": (512, 4), "m16n8k4": (1024, 4), "m16n8k8": (2048, 4), "m16n8k16": (4096, 4)}
+
+
+def dmma_peak_tflops(shape: str = "m8n8k4") -> float:
+    """FP64 tensor-core (DMMA) throughput of this GPU for one mma.sync f64
+    shape (TFLOP/s), CUDA events."""
     import torch
 
     lib = _peak_module()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    blocks, threads, iters = sms * 4, 256, 2048
+    flops, per_iter = DMMA_SHAPES[shape]
+    blocks, threads, iters = sms * 4, 256, max(256, 2048 * 512 // flops)
     out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
     best = 0.0
     for _ in range(3):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        lib.run_dmma(out, blocks, threads, iters)
+        lib.run_dmma(out, blocks, threads, iters, shape)
         e1.record()
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        best = max(best, 4.0 * 512.0 * iters * blocks * (threads // 32) / (ms * 1e9))
+        best = max(best, per_iter * float(flops) * iters * blocks * (threads // 32) / (ms * 1e9))
     return best
+
+
+def dmma_all_shapes() -> dict:
+    return {shape: round(dmma_peak_tflops(shape), 3) for shape in DMMA_SHAPES}
 
 
 _PEAK_LIB = None
@@ -235,8 +288,12 @@ extern "C" int launch_peak(double* out, int blocks, int threads, int iters, void
   dfma_peak<<<blocks, threads, 0, (cudaStream_t)st>>>(out, iters, 0.999, 1e-3);
   return (int)cudaGetLastError();
 }
-extern "C" int launch_dmma(double* out, int blocks, int threads, int iters, void* st) {
-  dmma_peak<<<blocks, threads, 0, (cudaStream_t)st>>>(out, iters);
+extern "C" int launch_dmma(double* out, int blocks, int threads, int iters, int shape, void* st) {
+  cudaStream_t s = (cudaStream_t)st;
+  if (shape == 0) dmma_peak<<<blocks, threads, 0, s>>>(out, iters);
+  else if (shape == 1) dmma_k4<<<blocks, threads, 0, s>>>(out, iters);
+  else if (shape == 2) dmma_k8<<<blocks, threads, 0, s>>>(out, iters);
+  else dmma_k16<<<blocks, threads, 0, s>>>(out, iters);
   return (int)cudaGetLastError();
 }
 """)
@@ -245,7 +302,8 @@ extern "C" int launch_dmma(double* out, int blocks, int threads, int iters, void
                     "-cudart", "shared", src, "-o", so], check=True, capture_output=True)
     lib = ctypes.CDLL(so)
     lib.launch_peak.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
-    lib.launch_dmma.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.launch_dmma.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                ctypes.c_void_p]
 
     class _M:
         @staticmethod
@@ -253,8 +311,9 @@ extern "C" int launch_dmma(double* out, int blocks, int threads, int iters, void
             lib.launch_peak(out.data_ptr(), blocks, threads, iters, torch.cuda.current_stream().cuda_stream)
 
         @staticmethod
-        def run_dmma(out, blocks, threads, iters):
-            lib.launch_dmma(out.data_ptr(), blocks, threads, iters, torch.cuda.current_stream().cuda_stream)
+        def run_dmma(out, blocks, threads, iters, shape="m8n8k4"):
+            lib.launch_dmma(out.data_ptr(), blocks, threads, iters, list(DMMA_SHAPES).index(shape),
+                            torch.cuda.current_stream().cuda_stream)
 
     _PEAK_LIB = _M
     return _M
@@ -307,27 +366,48 @@ def cpu_sample(n2_sample: int, n2_target: int, threads: int):
     return dt * 1e3 * scale, dt
 
 
+# The compiled reference timed directly at the headline size, once, on the
+# 8-core x86 development host (OpenBLAS 0.3.31, 8 threads): it cannot be built
+# on the GPU host (its sources stay out of this repository), so the bench's
+# reference arm extrapolates from a bounded sample and carries this figure
+# beside it, labelled.
+REFERENCE_MEASURED_N2_8192 = {"n2": 8192, "seconds": 412.0, "impl": "compiled reference (oracle/_ref)",
+                              "host": "8-core x86 development host, OpenBLAS 0.3.31, 8 threads",
+                              "measured_on_gpu_host": False}
+
+
+def cpu_baseline_fields(value_ms: float, n2_target: int, n2_sample: int, raw_s: float, threads: int) -> dict:
+    """The cpu_baseline object: what was timed, and how it was scaled."""
+    kind = cpu_kind()
+    scale = (n2_target / n2_sample) ** 3
+    return {"value": value_ms, "unit": "ms", "cores": threads, "kind": kind,
+            "sample": f"one n2={n2_sample} solve per step through "
+                      + ("oracle/_ref (the compiled reference, OpenBLAS)" if kind == "reference"
+                         else "oracle/port.py (numpy + scipy OpenBLAS/LAPACK restatement of the reference)")
+                      + f" = {raw_s:.2f} s, scaled x{scale:.0f} (n^3) to n2={n2_target}",
+            "extrapolated": n2_sample != n2_target, "sample_n2": n2_sample, "sample_s": round(raw_s, 3),
+            "scale_n3": scale, "fits_in_driver_run": n2_sample == n2_target,
+            "reference_measured_directly": REFERENCE_MEASURED_N2_8192}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     os.environ["OPENBLAS_NUM_THREADS"] = str(threads)
-    vals = []
+    vals, raws = [], []
     for i in range(args.warmup + args.steps):
         ms, raw = cpu_sample(args.cpu_sample_n2, args.n2, threads)
         if i >= args.warmup:
             vals.append(ms)
+            raws.append(raw)
     v = float(np.mean(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
         "config": workload_config(args.n2, world),
-        "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": cpu_kind(),
-                         "sample": f"one n2={args.cpu_sample_n2} solve per step through "
-                                   + ("oracle/_ref (the compiled reference, OpenBLAS)" if cpu_kind() == "reference"
-                                      else "oracle/port.py (numpy + scipy OpenBLAS/LAPACK)")
-                                   + f", x{(args.n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
+        "cpu_baseline": cpu_baseline_fields(v, args.n2, args.cpu_sample_n2, float(np.mean(raws)), threads),
         "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -828,14 +908,10 @@ def main():
             "stage_ms": {"refine": round(prof["refine"][0] / args.steps, 2), "ozaki": round(oz_ms, 2),
                          "fp32_decomposition": round(ms_step - prof["refine"][0] / args.steps, 2)},
             "fp64_path_roofline": {"pipe": "fp64 DFMA", "peak_tflops_measured": round(fp64_peak, 3),
-                                   "dmma_tflops_measured": round(dmma_peak_tflops(), 3),
+                                   "dmma_tflops_measured": dmma_all_shapes(),
                                    "kernels": fp64_roof},
             "accuracy": acc,
-            "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": os.cpu_count() or 1, "kind": cpu_kind(),
-                             "sample": f"one n2={args.cpu_sample_n2} solve through "
-                                       + ("oracle/_ref (the compiled reference, OpenBLAS)" if cpu_kind() == "reference"
-                                          else "oracle/port.py (numpy + scipy OpenBLAS/LAPACK)")
-                                       + f" = {cpu_raw:.2f} s, scaled x{(n2 / args.cpu_sample_n2) ** 3:.0f} (n^3)"},
+            "cpu_baseline": cpu_baseline_fields(cpu_ms, n2, args.cpu_sample_n2, cpu_raw, os.cpu_count() or 1),
             "clocks": clocks,
         }
         line["gpu_launches"] = int(launches)

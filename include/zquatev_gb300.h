@@ -112,6 +112,14 @@ int zq_get_block_size(void);
 int zq_set_ozaki_kernel(int which);
 int zq_get_ozaki_kernel(void);
 
+/* Limit, in SM clock cycles, of every wait of the tensor-core pipelines
+ * (mbarrier waits between the copy, MMA and drain roles); cycles <= 0 restores
+ * the default (about 2 s). When a wait runs out, the kernel stops issuing
+ * work, waits for what it already issued, frees its tensor memory and
+ * returns, and the call returns -104. A test hook for that path: no
+ * counterpart in the reference, which has no device code. */
+int zq_set_pipeline_wait(long long cycles);
+
 /* Panel-width autotuner: times the quaternion tridiagonalisation of a seeded
  * random matrix of order n2 for nb in {16, 32, 64} and stores the fastest for
  * n2's size bucket (powers of two of n) and precision (0: FP64 path, 1: FP32

@@ -33,6 +33,11 @@ def test_reference_arm_json_line():
     assert d["higher_is_better"] is False and d["unit"] == "ms" and d["value"] > 0
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert d["cpu_baseline"]["kind"] == bench_kind() and d["cpu_baseline"]["cores"] >= 1
+    # a scaled sample says so, with the sample and the factor
+    cb = d["cpu_baseline"]
+    assert cb["extrapolated"] is True and cb["sample_n2"] == 64 and cb["scale_n3"] == (8192 / 64) ** 3
+    assert cb["fits_in_driver_run"] is False
+    assert cb["reference_measured_directly"]["n2"] == 8192
 
     sys.path.insert(0, ROOT)
     import bench

@@ -20,7 +20,12 @@ from zquatev_gb300 import _lib, inputs, metrics, solver
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
-GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+GDIR = os.path.join(os.path.dirname(__file__), "golden")
+GOLDEN = sorted(glob.glob(os.path.join(GDIR, "random_*.npz")) + glob.glob(os.path.join(GDIR, "clustered_*.npz")))
+SKETCHED = sorted(glob.glob(os.path.join(GDIR, "sketch_*.npz")))
+# the three ways in: the plain FP64 path, the drop-in's own policy (refined
+# from n = 48 up: what ts::zquatev runs) and the refined path forced
+PATHS = {"fp64": solver.zquatev_fp64, "default": solver.zquatev, "refined": solver.zquatev_refined}
 
 
 def run(d, n2=None, ld2=None, sentinel=7.25, fn=None):
@@ -48,19 +53,45 @@ def check_solution(d, out, eig, n, ref_eig=None):
     return h
 
 
+@pytest.mark.parametrize("fn", list(PATHS), ids=list(PATHS))
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
-def test_against_reference_golden(gpu, path):
+def test_against_reference_golden(gpu, path, fn):
     z = np.load(path)
     left = z["left"]
     n = left.shape[1]
     d = np.zeros((2 * n, 2 * n), dtype=np.complex128, order="F")
     d[:, :n] = left
     d[:, n:] = 3.0 - 1.0j  # right half is ignored by the solver
-    out, eig = run(d)
+    out, eig = run(d, fn=PATHS[fn])
     assert np.all(eig[n:] == 7.25)  # eig[n..] untouched (reference behaviour)
     check_solution(d, out, eig, n, ref_eig=z["eig"])
     tol = 1e-6 * max(metrics.h_norm2(z["eig"]), 1.0)
     assert metrics.subspace_distance(out, eig[:n], z["out"], z["eig"], tol) < 1e-8
+    if fn == "refined" and str(z["kind"]) == "random" and n >= 20:
+        assert not solver.refine_stats()[2], "refined path fell back to FP64"
+
+
+@pytest.mark.parametrize("fn", list(PATHS), ids=list(PATHS))
+@pytest.mark.parametrize("path", SKETCHED, ids=[os.path.basename(p) for p in SKETCHED])
+def test_against_reference_sketched(gpu, path, fn):
+    """Config-size fixtures from the compiled reference (the n2 = 512 config-0
+    matrix, n2 = 1024 and 2048 random, n2 = 512 clustered): eigenvalues against
+    the reference's, invariant subspaces against its eigenvectors through the
+    stored sketch, plus residual, orthonormality and exact structure."""
+    from tests.golden import make_golden
+
+    z = np.load(path)
+    n, kind, seed = int(z["n"]), str(z["kind"]), int(z["seed"])
+    d = make_golden.sketched_input(kind, n, seed)
+    assert np.allclose(make_golden.input_checksum(d[:, :n]), z["checksum"], rtol=1e-12, atol=1e-12)
+    out, eig = run(d, fn=PATHS[fn])
+    assert np.all(eig[n:] == 7.25)
+    check_solution(d, out, eig, n, ref_eig=z["eig"])
+    hn = metrics.h_norm2(z["eig"])
+    s = metrics.sketch_matrix(2 * n, int(z["sketch_k"]), int(z["sketch_seed"]))
+    assert metrics.sketch_distance(out, eig[:n], z["sketch"], z["eig"], s, 1e-5 * max(hn, 1.0)) < 1e-8
+    if fn == "refined" and kind == "random":
+        assert not solver.refine_stats()[2], "refined path fell back to FP64"
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 20, 21, 22, 31, 32, 33, 63, 64, 65, 97, 128, 200])
@@ -329,3 +360,56 @@ def test_host_memory_kinds(gpu, memory, monkeypatch):
     assert np.all(d[n2:, :] == 123.0)
     assert np.all(eig[n:] == 7.25)
     check_solution(d0, np.asarray(d[:n2]), eig, n)
+
+
+def _device_solve(fn_name, dmaster, n2):
+    import torch
+
+    dt = dmaster.clone()
+    de = torch.full((n2,), 7.25, dtype=torch.float64, device="cuda")
+    lib = _lib.load()
+    st = torch.cuda.current_stream().cuda_stream
+    if fn_name == "refined":
+        rc = lib.zquatev_refined_device(n2, dt.data_ptr(), n2, de.data_ptr(), st, 1)
+    else:
+        rc = lib.zquatev_fp64_device(n2, dt.data_ptr(), n2, de.data_ptr(), st)
+    torch.cuda.synchronize()
+    assert rc == 0, (rc, _lib.last_error())
+    return dt, de
+
+
+@pytest.mark.parametrize("n2,kind", [(8192, "random"), (4096, "clustered")], ids=["config1_n2-8192", "config3_n2-4096"])
+def test_refined_vs_fp64_at_scale(gpu, n2, kind):
+    """At the config sizes the default (refined) path agrees with the plain FP64
+    GPU path: eigenvalues within 1e-12 ||H||, residual and orthonormality of the
+    refined result <= 1e-12, exact structure. The n2 = 8192 matrix is the
+    config-1 workload; the clustered one has config 3's spectrum (20% in
+    clusters of 8 with 1e-6 gaps) at half its size. Checks run on the GPU in
+    FP64 (torch), as numpy would take minutes."""
+    import torch
+
+    n = n2 // 2
+    if kind == "random":
+        d = inputs.random_matrix(n, 20240)
+        dmaster = torch.from_numpy(np.ascontiguousarray(d.T)).cuda()
+        del d
+    else:
+        dmaster, _ = inputs.clustered_matrix_device(n, 4100)
+    h = dmaster.T.clone()  # column-major view of D: the left half holds [A; B]
+    a, b = h[:n, :n], h[n:, :n]
+    hfull = torch.empty((n2, n2), dtype=torch.complex128, device="cuda")
+    hfull[:n, :n], hfull[n:, :n], hfull[:n, n:], hfull[n:, n:] = a, b, -b.conj(), a.conj()
+    del h, a, b
+    r_out, r_eig = _device_solve("refined", dmaster, n2)
+    f_out, f_eig = _device_solve("fp64", dmaster, n2)
+    assert bool((r_eig[n:] == 7.25).all())
+    hn = float(f_eig[:n].abs().max())
+    assert float((r_eig[:n] - f_eig[:n]).abs().max()) / hn <= TOL
+    assert bool((r_eig[1:n] >= r_eig[:n - 1]).all())
+    v = r_out.T  # column-major: columns are eigenvectors
+    assert metrics.torch_residual(hfull, v, r_eig[:n]) <= TOL
+    assert metrics.torch_orthonormality(v) <= TOL
+    u, w = v[:n, :n], v[n:, :n]
+    assert bool((v[:n, n:] == -w.conj()).all()) and bool((v[n:, n:] == u.conj()).all())
+    if kind == "random":
+        assert not solver.refine_stats()[2], "refined path fell back to FP64"

@@ -113,3 +113,41 @@ def test_refined_converges_without_fallback(gpu, n):
     ref = np.linalg.eigvalsh(h)[::2]
     assert metrics.eig_error(eig[:n], ref, metrics.h_norm2(ref)) <= TOL
     assert metrics.residual(h, out, eig[:n]) <= TOL
+
+
+def _accurate_product(lib, m, n, k, seed):
+    import torch
+
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    b = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    da = torch.from_numpy(np.ascontiguousarray(a.T)).cuda()
+    db = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()
+    dc = torch.zeros((n, m), dtype=torch.complex128, device="cuda")
+    rc = lib.zq_zgemm_accurate(0, 0, m, n, k, da.data_ptr(), m, db.data_ptr(), k, dc.data_ptr(), m,
+                               torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return rc, a, b, dc.cpu().numpy().T
+
+
+def test_pipeline_wait_timeout_reports_and_recovers(gpu):
+    """A tcgen05 pipeline wait that runs out (a limit of a few hundred cycles,
+    far below one tensor-memory copy) stops the kernel cleanly: the call returns
+    -104 with its message, the device keeps answering, and the next call at the
+    default limit is correct."""
+    import torch
+
+    assert gpu.zq_set_ozaki_kernel(1) == 0
+    try:
+        assert gpu.zq_set_pipeline_wait(300) == 0
+        rc, _, _, _ = _accurate_product(gpu, 256, 256, 256, 5)
+        assert rc == -104, (rc, _lib.last_error())
+        assert "ran out of time" in _lib.last_error()
+    finally:
+        gpu.zq_set_pipeline_wait(0)
+    assert float(torch.ones(1024, device="cuda").sum()) == 1024.0  # the context still answers
+    rc, a, b, c = _accurate_product(gpu, 256, 256, 256, 5)
+    assert rc == 0, _lib.last_error()
+    exact = a.astype(np.clongdouble) @ b.astype(np.clongdouble)
+    err = np.abs(c - exact.astype(np.complex128)) / (np.abs(a) @ np.abs(b))
+    assert err.max() < 2e-15

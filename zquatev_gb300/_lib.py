@@ -43,6 +43,7 @@ SIGNATURES = {
     "zq_autotune_nb": (_c_int, [_c_int, _c_int, _vp, _vp]),
     "zq_set_ozaki_kernel": (_c_int, [_c_int]),
     "zq_get_ozaki_kernel": (_c_int, []),
+    "zq_set_pipeline_wait": (_c_int, [_c_ll]),
     "zq_tuned_nb": (_c_int, [_c_int, _c_int]),
     "zq_set_tuned_nb": (_c_int, [_c_int, _c_int, _c_int]),
     "zq_batch_plan_create": (_vp, [_c_int, _vp, _vp, _vp, _vp, _c_int]),

@@ -739,6 +739,11 @@ const char* zq_last_error(void) { return last_error_message(); }
 
 int zq_version(void) { return 100; }
 
+int zq_set_pipeline_wait(long long cycles) {
+  zq::set_pipeline_wait_cycles(cycles);
+  return ZQ_OK;
+}
+
 long long zq_launch_count(void) { return zq::g_launches.load(std::memory_order_relaxed); }
 
 int zq_release_workspace(void) {

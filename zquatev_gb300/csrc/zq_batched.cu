@@ -474,10 +474,17 @@ extern "C" int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig,
   BatchTask tk{};
   tk.off = 0; tk.eoff = 0; tk.Dp = nullptr; tk.Ep = nullptr; tk.n = n2 / 2; tk.ld = ld2; tk.out_slot = 0;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  (void)cudaGetLastError();  // an earlier, unrelated launch error of the caller is not this call's
   k_solve_small_noalloc<<<1, BT, 0, st>>>(tk, reinterpret_cast<double2*>(dD), deig, scratch, info_dev);
-  ZQ_CUDA(cudaGetLastError());
+  ZQ_CUDA(cudaGetLastError());  // the launch itself failed: nothing was enqueued
+  count_launch();
+  // From here the kernel is queued: whatever happens, wait for the stream
+  // before returning, so that no error return leaves it writing D, eig or the
+  // shared scratch behind the caller's back.
   int info = 0;
-  ZQ_CUDA(cudaMemcpyAsync(&info, info_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
-  ZQ_CUDA(cudaStreamSynchronize(st));
+  const cudaError_t ce = cudaMemcpyAsync(&info, info_dev, sizeof(int), cudaMemcpyDeviceToHost, st);
+  const cudaError_t se = cudaStreamSynchronize(st);
+  if (ce != cudaSuccess) { set_last_error(ce, "cudaMemcpyAsync(info)", __FILE__, __LINE__); return ZQ_ERR_CUDA; }
+  if (se != cudaSuccess) { set_last_error(se, "cudaStreamSynchronize", __FILE__, __LINE__); return ZQ_ERR_CUDA; }
   return info;
 }

@@ -175,6 +175,10 @@ struct OzOpts {
 int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st,
                 const OzOpts& opt);
 size_t ozaki_workspace_bytes(int n);
+// limit of every mbarrier wait in the tensor-core pipelines, SM clock cycles
+// (<= 0: the default, about 2 s); a test hook for the timeout path
+void set_pipeline_wait_cycles(long long cycles);
+long long pipeline_wait_cycles();
 // upper triangle of a square structured matrix from its lower triangle (sym +1 Hermitian, -1 antisymmetric)
 int structured_fill(double2* C, int64_t ldc, int n, int sym, cudaStream_t st);
 

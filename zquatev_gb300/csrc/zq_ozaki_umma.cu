@@ -21,10 +21,11 @@
 // The accumulators are double buffered, so draining one overlaps the MMAs
 // into the other.
 //
-// Every wait on an mbarrier is bounded (about 2 s). On a timeout the kernel
-// raises the error flag the host reads after the launch, stops issuing work,
-// waits (bounded) for its own copies and MMAs in flight, frees its TMEM and
-// returns.
+// Every wait on an mbarrier is bounded (default about 2 s of SM clock; the
+// limit is a kernel argument, set by zq_set_pipeline_wait). On a timeout the
+// kernel raises the error flag the host reads after the launch, stops issuing
+// work, waits (bounded, always at the default limit) for its own copies and
+// MMAs in flight, frees its TMEM and returns.
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
@@ -51,7 +52,7 @@ constexpr uint32_t UM_BH_BYTES = UM_BN * UM_BK * 2;      // 16 KB (Bre or Bim ha
 constexpr uint32_t UM_STAGE_BYTES = UM_A_BYTES + 2 * UM_BH_BYTES;
 constexpr uint32_t UM_TMEM_COLS = 512;
 constexpr int UM_SMEM = 1024 + UM_STAGES * UM_STAGE_BYTES + 256;
-constexpr long long UM_WAIT_CYCLES = 4000000000LL;  // about 2 s of SM clock
+constexpr long long UM_WAIT_CYCLES = 4000000000LL;  // default wait limit: about 2 s of SM clock
 // kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N = 256, M = 128
 constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
 
@@ -62,6 +63,7 @@ struct UmArgs {
   double2* C;
   int64_t ldc;
   int* err;
+  long long wait;  // limit of every pipeline wait, SM clock cycles
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -84,17 +86,18 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase with the given parity. False when the time limit
-// passes (the abort flag is raised) or when another role has aborted.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort) {
+// Bounded wait for the phase with the given parity. False when `limit` cycles
+// pass (the abort flag is raised) or when another role has aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort, long long limit) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity)) {
     if (*abort) return false;
-    if (clock64() - t0 > UM_WAIT_CYCLES) { *abort = 1; return false; }
+    if (clock64() - t0 > limit) { *abort = 1; return false; }
   }
   return true;
 }
-// Bounded wait that ignores the abort flag (clean-up of work in flight).
+// Bounded wait that ignores the abort flag (clean-up of work in flight): always
+// the default limit, as copies and MMAs already issued finish in microseconds.
 __device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity) && clock64() - t0 <= UM_WAIT_CYCLES) {
@@ -206,7 +209,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
         const int64_t total = (int64_t)(lev + 1) * Kp;
         for (int64_t kg = 0; kg < total && ok; kg += UM_BK) {
           const int stage = ks % UM_STAGES, round = ks / UM_STAGES;
-          if (!mbar_wait(empty0 + 8 * stage, (round & 1) ^ 1, abort)) { ok = false; break; }
+          if (!mbar_wait(empty0 + 8 * stage, (round & 1) ^ 1, abort, g.wait)) { ok = false; break; }
           const uint32_t sA = ring + stage * UM_STAGE_BYTES;
           const int t = (int)(kg / Kp), kk = (int)(kg % Kp), u = lev - t;
           mbar_expect_tx(full0 + 8 * stage, UM_STAGE_BYTES);
@@ -233,12 +236,12 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
           for (int64_t cb = kbeg; cb < kend && ok; cb += UM_CH) {
             const int64_t ce = cb + UM_CH < kend ? cb + UM_CH : kend;
             const int buf = ci & 1;
-            if (!mbar_wait(acce0 + 8 * buf, ((ci >> 1) & 1) ^ 1, abort)) { ok = false; break; }
+            if (!mbar_wait(acce0 + 8 * buf, ((ci >> 1) & 1) ^ 1, abort, g.wait)) { ok = false; break; }
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(buf * 256);
             for (int64_t kg = cb; kg < ce; kg += UM_BK) {
               const int stage = ks % UM_STAGES, round = ks / UM_STAGES;
-              if (!mbar_wait(full0 + 8 * stage, round & 1, abort)) { ok = false; break; }
+              if (!mbar_wait(full0 + 8 * stage, round & 1, abort, g.wait)) { ok = false; break; }
               tc_fence_after();
               const uint32_t sA = ring + stage * UM_STAGE_BYTES;
               const uint64_t ad = sw128_desc(sA), bd = sw128_desc(sA + UM_A_BYTES);
@@ -277,7 +280,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
         for (int64_t cb = kbeg; cb < kend; cb += UM_CH) {
           const int buf = ci & 1;
           // warp-uniform outcome: the TMEM loads below are .sync.aligned
-          const bool got = mbar_wait(accf0 + 8 * buf, (ci >> 1) & 1, abort);
+          const bool got = mbar_wait(accf0 + 8 * buf, (ci >> 1) & 1, abort, g.wait);
           if (!__all_sync(0xffffffffu, got)) { ok = false; break; }
           tc_fence_after();
           const uint32_t base = lane_base + (uint32_t)(buf * 256 + 64 * h);
@@ -359,9 +362,14 @@ int make_map(CUtensorMap* tm, const __nv_bfloat16* base, int64_t Kp, int64_t row
   return ZQ_OK;
 }
 
+std::atomic<long long> g_wait_cycles{UM_WAIT_CYCLES};
+
 }  // namespace
 
 int oz_umma_smem_bytes() { return UM_SMEM; }
+
+void set_pipeline_wait_cycles(long long cycles) { g_wait_cycles.store(cycles > 0 ? cycles : UM_WAIT_CYCLES); }
+long long pipeline_wait_cycles() { return g_wait_cycles.load(); }
 
 // C (m x n, FP64 complex) from the slices (layout [S][rows padded to 128][Kp]);
 // err: device int, zeroed here, raised by the kernel on a wait timeout.
@@ -386,6 +394,7 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
   UmArgs a{};
   a.mp = mp; a.np = np; a.Kp = Kp; a.m = m; a.n = n; a.nsl = nsl; a.lower = lower;
   a.ea = ea; a.eb = eb; a.C = C; a.ldc = ldc; a.err = err;
+  a.wait = g_wait_cycles.load();
   const int tm = mp / UM_BM, tn = np / UM_BN;
   const dim3 grid = lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)(tm * tn), 1);
   ZQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));

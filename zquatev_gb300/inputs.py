@@ -18,9 +18,48 @@ from __future__ import annotations
 import numpy as np
 
 
-def random_blocks(n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+class PortableRNG:
+    """Counter-based generator (splitmix64 + Box-Muller) whose stream depends
+    only on the seed: the same numbers on every machine and numpy version (up
+    to the last bit of log/cos), so large fixtures can store a seed instead of
+    their input. Offers the subset of numpy's Generator the workloads use."""
+
+    _GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+
+    def __init__(self, seed: int):
+        self._seed = np.uint64(seed & 0xFFFFFFFFFFFFFFFF)
+        self._ctr = 0
+
+    def _u64(self, count: int) -> np.ndarray:
+        i = np.arange(self._ctr + 1, self._ctr + 1 + count, dtype=np.uint64)
+        self._ctr += count
+        with np.errstate(over="ignore"):
+            z = self._seed + i * self._GOLDEN
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+    def random(self, size) -> np.ndarray:
+        count = int(np.prod(size))
+        u = ((self._u64(count) >> np.uint64(11)).astype(np.float64) + 0.5) * 2.0 ** -53  # in (0, 1)
+        return u.reshape(size)
+
+    def uniform(self, lo: float, hi: float, size) -> np.ndarray:
+        return lo + (hi - lo) * self.random(size)
+
+    def standard_normal(self, size) -> np.ndarray:
+        u1 = self.random(size)
+        u2 = self.random(size)
+        return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def make_rng(seed: int, portable: bool = False):
+    return PortableRNG(seed) if portable else np.random.default_rng(seed)
+
+
+def random_blocks(n: int, seed: int, portable: bool = False) -> tuple[np.ndarray, np.ndarray]:
     """A (Hermitian) and B (antisymmetric), n x n complex128."""
-    rng = np.random.default_rng(seed)
+    rng = make_rng(seed, portable)
     x = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
     y = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
     a = (x + x.conj().T) / 2
@@ -60,19 +99,19 @@ def pack_left_half(a: np.ndarray, b: np.ndarray, ld2: int | None = None,
     return d
 
 
-def random_matrix(n: int, seed: int, ld2: int | None = None) -> np.ndarray:
-    a, b = random_blocks(n, seed)
+def random_matrix(n: int, seed: int, ld2: int | None = None, portable: bool = False) -> np.ndarray:
+    a, b = random_blocks(n, seed, portable)
     return pack_left_half(a, b, ld2)
 
 
-def quaternion_unitary(n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+def quaternion_unitary(n: int, seed: int, portable: bool = False) -> tuple[np.ndarray, np.ndarray]:
     """Left half [Q0; Q1] of a Haar-like random quaternion-unitary 2n x 2n Q.
 
     Built by structure-preserving Gram-Schmidt on a complex Gaussian in
     quaternion form: column j is orthogonalised (twice) against the previous
     columns and their quaternion partners J*conj(q) = (-conj(q1); conj(q0)).
     """
-    rng = np.random.default_rng(seed)
+    rng = make_rng(seed, portable)
     g = rng.standard_normal((2 * n, n)) + 1j * rng.standard_normal((2 * n, n))
     q = np.zeros((2 * n, n), dtype=np.complex128)
     for j in range(n):
@@ -88,8 +127,8 @@ def quaternion_unitary(n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
 
 
 def clustered_spectrum(n: int, seed: int, gap: float = 1e-6,
-                       cluster: int = 8, frac: float = 0.2) -> np.ndarray:
-    rng = np.random.default_rng(seed + 7919)
+                       cluster: int = 8, frac: float = 0.2, portable: bool = False) -> np.ndarray:
+    rng = make_rng(seed + 7919, portable)
     ncl = int(round(frac * n)) // cluster
     nfree = n - ncl * cluster
     lam = list(rng.uniform(-10.0, 10.0, nfree))
@@ -98,11 +137,11 @@ def clustered_spectrum(n: int, seed: int, gap: float = 1e-6,
     return np.sort(np.asarray(lam))
 
 
-def clustered_matrix(n: int, seed: int, ld2: int | None = None
+def clustered_matrix(n: int, seed: int, ld2: int | None = None, portable: bool = False
                      ) -> tuple[np.ndarray, np.ndarray]:
     """(D, lambda): H = Q diag(lambda) Q^H in quaternion form, plus its spectrum."""
-    q0, q1 = quaternion_unitary(n, seed)
-    lam = clustered_spectrum(n, seed)
+    q0, q1 = quaternion_unitary(n, seed, portable)
+    lam = clustered_spectrum(n, seed, portable=portable)
     # H = Qf diag(lam, lam) Qf^H with Qf = (Q0 -Q1*; Q1 Q0*); left half only.
     a = (q0 * lam) @ q0.conj().T + (q1.conj() * lam) @ q1.T
     b = (q1 * lam) @ q0.conj().T - (q0.conj() * lam) @ q1.T

@@ -80,3 +80,47 @@ def torch_orthonormality(v):
     g = v.conj().T @ v
     g.diagonal().sub_(1.0)
     return float(g.abs().max())
+
+
+def sketch_matrix(n2: int, k: int = 4, seed: int = 0):
+    """(n2, k) complex Gaussian probe S (re, im ~ N(0, 1)) from the portable generator."""
+    from .inputs import PortableRNG
+
+    rng = PortableRNG(seed)
+    return rng.standard_normal((n2, k)) + 1j * rng.standard_normal((n2, k))
+
+
+def sketch(v: np.ndarray, s: np.ndarray) -> np.ndarray:
+    """W = V^H S: a compact fingerprint of the eigenvector matrix V (n2 x n2)."""
+    return v.conj().T @ s
+
+
+def sketch_distance(v: np.ndarray, eig: np.ndarray, w_ref: np.ndarray, eig_ref: np.ndarray,
+                    s: np.ndarray, tol: float) -> float:
+    """Subspace comparison against a reference known only through W_ref = V_ref^H S.
+
+    For each cluster C of eigenvalues closer than ``tol`` (both Kramers partners,
+    columns i and i + n), W_C^H W_C = S^H P_C S with P_C the projector onto the
+    cluster's invariant subspace: independent of the quaternion phases and of any
+    rotation inside the cluster. Returns the largest entry of
+    |S^H (P_C - P_C,ref) S| over the clusters, divided by mean |s_i|^2 (= 2 for
+    unit complex Gaussians): of the order of the sine of the largest principal
+    angle between the two subspaces.
+    """
+    n = eig.size
+    scale = float(np.mean(np.abs(s) ** 2))
+    order = np.argsort(eig)
+    w = v.conj().T @ s
+    worst = 0.0
+    i = 0
+    while i < n:
+        j = i + 1
+        while j < n and eig[order[j]] - eig[order[j - 1]] <= tol:
+            j += 1
+        cols = np.concatenate([order[i:j], order[i:j] + n])
+        rcols = np.concatenate([np.arange(i, j), np.arange(i, j) + n])
+        k_out = w[cols].conj().T @ w[cols]
+        k_ref = w_ref[rcols].conj().T @ w_ref[rcols]
+        worst = max(worst, float(np.max(np.abs(k_out - k_ref))) / scale)
+        i = j
+    return worst
