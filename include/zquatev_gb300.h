@@ -120,6 +120,17 @@ int zq_get_ozaki_kernel(void);
  * counterpart in the reference, which has no device code. */
 int zq_set_pipeline_wait(long long cycles);
 
+/* FP32-accurate product on the tcgen05 tensor cores (TF32, three passes:
+ * hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory), the kernel of
+ * the refined path's Q formation, back-transform and large divide-and-conquer
+ * merges (the reference forms those products with zgemm3m: blocked.cc:477-544,
+ * zquatev.cc:86-90). C = op(A) op(B), column-major, complex64 (cplx = 1; op 0
+ * N, 1 T, 2 conjugate transpose, 3 conjugate) or float32 (cplx = 0; op 0 N,
+ * 1 T); splits > 1 divides K over that many CTAs per tile. Device pointers;
+ * waits for `stream`. */
+int zq_gemm_tf32x3(int cplx, int opa, int opb, int m, int n, int k, const float* A, int lda, const float* B,
+                   int ldb, float* C, int ldc, int splits, void* stream);
+
 /* Panel-width autotuner: times the quaternion tridiagonalisation of a seeded
  * random matrix of order n2 for nb in {16, 32, 64} and stores the fastest for
  * n2's size bucket (powers of two of n) and precision (0: FP64 path, 1: FP32

@@ -44,6 +44,8 @@ SIGNATURES = {
     "zq_set_ozaki_kernel": (_c_int, [_c_int]),
     "zq_get_ozaki_kernel": (_c_int, []),
     "zq_set_pipeline_wait": (_c_int, [_c_ll]),
+    "zq_gemm_tf32x3": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp, _c_int, _vp, _c_int, _vp, _c_int,
+                                _c_int, _vp]),
     "zq_tuned_nb": (_c_int, [_c_int, _c_int]),
     "zq_set_tuned_nb": (_c_int, [_c_int, _c_int, _c_int]),
     "zq_batch_plan_create": (_vp, [_c_int, _vp, _vp, _vp, _vp, _c_int]),

@@ -21,6 +21,9 @@
 //   4. symmetry_fill: D[:, n:] = (-conj(V); conj(U)).
 #include "zq_common.cuh"
 #include "zq_kernels.h"
+#include "zq_tc32.h"
+
+#include <type_traits>
 
 namespace zq {
 
@@ -181,12 +184,21 @@ size_t form_q_workspace_bytes(int n, int nbq) {
   return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n + (size_t)fq_pcap(n, nbq)) + 256;
 }
 
+// Operand source of the tensor-core product (zq_tc32.cu) over a complex64 array.
+static Tc32Src tsrc(const float2* p, int64_t ld, int kfast, int conj = 0, float sign = 1.f) {
+  Tc32Src s{};
+  s.p = reinterpret_cast<const float*>(p); s.ld = ld; s.kfast = kfast; s.conj = conj; s.sign = sign;
+  return s;
+}
+
 template <typename R>
 int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, int64_t ldx, int nbq, void* ws,
-           cudaStream_t st) {
+           cudaStream_t st, int* tc_err) {
   using Z = cplx<R>;
   using Args = ZgemmArgsT<R>;
   if (n <= 0) return ZQ_OK;
+  // FP32 path: the two large products per block on the tensor cores
+  const bool use_tc = std::is_same<R, float>::value && tc_err != nullptr && fp32_products_on_tensor_cores(TC_USE_FORMQ);
   k_init_x<Z><<<ceil_div(2 * n * n, 256) > 4096 ? 4096 : ceil_div(2 * n * n, 256), 256, 0, st>>>(X, ldx, n, phi);
   ZQ_LAUNCH_CHECK();
   const int nref = n - 2;  // reflectors exist for columns 0..n-3
@@ -233,28 +245,89 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
     // C1e = Wa^H Xa_sub + Wb^H Xb_sub ; C1o = Wa^T Xb_sub - Wb^T Xa_sub   (kb x L)
     Z* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
     Z* Xbs = Xb + (pb + 1) + (int64_t)(pb + 1) * ldx;
-    g = Args{};
-    g.P = Pk; g.pcap = pcap;
-    g.m = kb; g.n = L; g.k1 = L; g.k2 = L;
-    g.A1 = Wa; g.lda1 = L; g.B1 = Xas; g.ldb1 = ldx;
-    g.A2 = Wb; g.lda2 = L; g.B2 = Xbs; g.ldb2 = ldx;
-    g.s2 = (R)1; g.alpha = one; g.beta = zero;
-    g.C = C1e; g.ldc = kb;
-    if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
-    g.A1 = Wa; g.B1 = Xbs; g.A2 = Wb; g.B2 = Xas; g.s2 = (R)-1; g.C = C1o;
-    if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
+    Z* C1eu = C1e;
+    Z* C1ou = C1o;
+    int64_t ldc1 = kb;
+    if (use_tc) {
+      if constexpr (std::is_same<R, float>::value) {
+        // both halves in one tensor-core product, formed transposed so that the
+        // long inner dimension L is contiguous in X and W:
+        //   [C1e; C1o]^T (L x 2kb) = [Xa_sub^T | Xb_sub^T] [[conj(Wa), -Wb]; [conj(Wb), Wa]]
+        // stored as C1 = [C1e; C1o] (2kb x L, ld 2kb) in the C1e/C1o area
+        ldc1 = 2 * kb;
+        C1eu = C1e;
+        C1ou = C1e + kb;
+        Tc32Args t{};
+        t.cplx = 1; t.m = L; t.n = 2 * kb; t.nseg = 2;
+        t.seg[0].a = tsrc(Xas, ldx, 1);
+        t.seg[0].b = tsrc(Wa, L, 1, 1);
+        t.seg[0].b2 = tsrc(Wb, L, 1, 0, -1.f);
+        t.seg[0].nsplit = kb; t.seg[0].k = L;
+        t.seg[1].a = tsrc(Xbs, ldx, 1);
+        t.seg[1].b = tsrc(Wb, L, 1, 1);
+        t.seg[1].b2 = tsrc(Wa, L, 1);
+        t.seg[1].nsplit = kb; t.seg[1].k = L;
+        t.alpha = make_float2(1.f, 0.f); t.beta = make_float2(0.f, 0.f);
+        t.C = reinterpret_cast<float*>(C1e); t.ldc = ldc1; t.ctrans = 1;
+        // split K over enough CTAs to fill the GPU (partials in the split-K buffer)
+        const int tiles = ceil_div(L, 128), kblk = 2 * ceil_div(L, 16);
+        int splits = 1;
+        while (tiles * splits < 2 * 152 && kblk / (2 * splits) >= 4 && (int64_t)(2 * splits) * L * 2 * kb <= pcap) splits *= 2;
+        t.splits = splits;
+        t.P = reinterpret_cast<float*>(Pk);
+        t.err = tc_err;
+        prof_begin(PC_FORMQ_GEMM, st);
+        const int rc = tc32_gemm(t, st);
+        prof_end(PC_FORMQ_GEMM, st);
+        if (rc) return rc;
+      }
+    } else {
+      g = Args{};
+      g.P = Pk; g.pcap = pcap;
+      g.m = kb; g.n = L; g.k1 = L; g.k2 = L;
+      g.A1 = Wa; g.lda1 = L; g.B1 = Xas; g.ldb1 = ldx;
+      g.A2 = Wb; g.lda2 = L; g.B2 = Xbs; g.ldb2 = ldx;
+      g.s2 = (R)1; g.alpha = one; g.beta = zero;
+      g.C = C1e; g.ldc = kb;
+      if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
+      g.A1 = Wa; g.B1 = Xbs; g.A2 = Wb; g.B2 = Xas; g.s2 = (R)-1; g.C = C1o;
+      if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
+    }
     // C2e = Ta C1e - conj(Tb) C1o ; C2o = Tb C1e + conj(Ta) C1o   (kb x L)
     g = Args{};
     g.P = Pk; g.pcap = pcap;
     g.m = kb; g.n = L; g.k1 = kb; g.k2 = kb;
-    g.A1 = Ta; g.lda1 = kb; g.B1 = C1e; g.ldb1 = kb;
-    g.A2 = Tb; g.lda2 = kb; g.B2 = C1o; g.ldb2 = kb;
+    g.A1 = Ta; g.lda1 = kb; g.B1 = C1eu; g.ldb1 = ldc1;
+    g.A2 = Tb; g.lda2 = kb; g.B2 = C1ou; g.ldb2 = ldc1;
     g.s2 = (R)-1; g.alpha = one; g.beta = zero;
     g.C = C2e; g.ldc = kb;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
     g.A1 = Tb; g.A2 = Ta; g.s2 = (R)1; g.C = C2o;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
     // Xa_sub -= Wa C2e - conj(Wb) C2o ; Xb_sub -= Wb C2e + conj(Wa) C2o   (L x L)
+    if (use_tc) {
+      if constexpr (std::is_same<R, float>::value) {
+        for (int half = 0; half < 2; ++half) {
+          Tc32Args t{};
+          t.cplx = 1; t.m = L; t.n = L; t.nseg = 2;
+          t.seg[0].a = tsrc(half ? Wb : Wa, L, 0);
+          t.seg[0].b = tsrc(C2e, kb, 1);
+          t.seg[0].k = kb;
+          t.seg[1].a = tsrc(half ? Wa : Wb, L, 0, 1, half ? 1.f : -1.f);
+          t.seg[1].b = tsrc(C2o, kb, 1);
+          t.seg[1].k = kb;
+          t.alpha = make_float2(-1.f, 0.f); t.beta = make_float2(1.f, 0.f);
+          t.C = reinterpret_cast<float*>(half ? Xbs : Xas); t.ldc = ldx;
+          t.splits = 1;
+          t.err = tc_err;
+          prof_begin(PC_FORMQ_GEMM, st);
+          const int rc = tc32_gemm(t, st);
+          prof_end(PC_FORMQ_GEMM, st);
+          if (rc) return rc;
+        }
+      }
+      continue;
+    }
     g = Args{};
     g.P = Pk; g.pcap = pcap;
     g.m = L; g.n = L; g.k1 = kb; g.k2 = kb;
@@ -271,8 +344,27 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
 
 template <typename R>
 int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<R>* out, int64_t ldo,
-            DgemmDescT<R>* dev_desc, cudaStream_t st) {
+            DgemmDescT<R>* dev_desc, cudaStream_t st, int* tc_err) {
   if (n <= 0) return ZQ_OK;
+  if constexpr (std::is_same<R, float>::value) {
+    if (tc_err && fp32_products_on_tensor_cores(TC_USE_APPLYZ)) {
+      // one real product on the tensor cores: (4n x n) real view of X times Z
+      Tc32Args t{};
+      t.cplx = 0; t.m = 4 * n; t.n = n; t.nseg = 1;
+      t.seg[0].a.p = reinterpret_cast<const float*>(X); t.seg[0].a.ld = 2 * ldx; t.seg[0].a.kfast = 0;
+      t.seg[0].a.sign = 1.f;
+      t.seg[0].b.p = Z; t.seg[0].b.ld = ldz; t.seg[0].b.kfast = 1; t.seg[0].b.sign = 1.f;
+      t.seg[0].k = n;
+      t.alpha = make_float2(1.f, 0.f); t.beta = make_float2(0.f, 0.f);
+      t.C = reinterpret_cast<float*>(out); t.ldc = 2 * ldo;
+      t.splits = 1;
+      t.err = tc_err;
+      prof_begin(PC_APPLYZ, st);
+      const int rc = tc32_gemm(t, st);
+      prof_end(PC_APPLYZ, st);
+      return rc;
+    }
+  }
   DgemmDescT<R> d{};
   d.A = reinterpret_cast<const R*>(X); d.lda = 2 * ldx;
   d.B = Z; d.ldb = ldz;
@@ -285,10 +377,10 @@ int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<
   return rc;
 }
 
-template int form_q<double>(const cplx<double>*, int64_t, int, const double*, cplx<double>*, int64_t, int, void*, cudaStream_t);
-template int form_q<float>(const cplx<float>*, int64_t, int, const double*, cplx<float>*, int64_t, int, void*, cudaStream_t);
-template int apply_z<double>(const cplx<double>*, int64_t, const double*, int64_t, int, cplx<double>*, int64_t, DgemmDescT<double>*, cudaStream_t);
-template int apply_z<float>(const cplx<float>*, int64_t, const float*, int64_t, int, cplx<float>*, int64_t, DgemmDescT<float>*, cudaStream_t);
+template int form_q<double>(const cplx<double>*, int64_t, int, const double*, cplx<double>*, int64_t, int, void*, cudaStream_t, int*);
+template int form_q<float>(const cplx<float>*, int64_t, int, const double*, cplx<float>*, int64_t, int, void*, cudaStream_t, int*);
+template int apply_z<double>(const cplx<double>*, int64_t, const double*, int64_t, int, cplx<double>*, int64_t, DgemmDescT<double>*, cudaStream_t, int*);
+template int apply_z<float>(const cplx<float>*, int64_t, const float*, int64_t, int, cplx<float>*, int64_t, DgemmDescT<float>*, cudaStream_t, int*);
 
 __global__ void k_symfill(double2* D, int64_t ld, int n) {
   const int64_t total = (int64_t)n * n;

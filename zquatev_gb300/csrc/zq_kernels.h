@@ -32,6 +32,7 @@ struct TridiagView {
   double* d;       // diagonal (n)
   double* e;       // quaternion subdiagonal (4 doubles each, n)
   double* tau;     // 1 if reflector j exists else 0 (n)
+  int* tc_err;     // FP32: tensor-core products allowed (their timeout flag); null: CUDA cores only
 };
 
 template <typename R>
@@ -92,6 +93,7 @@ struct DcPlan {
   int max_depth = 0;
   std::vector<DcNode> nodes_host;
   std::vector<int> depth_off, depth_cnt, leaf_off, leaf_cnt;
+  std::vector<int> depth_mmax;  // largest node (b - a) per depth
   std::vector<DgemmDesc> gemm_host;
   std::vector<int> gemm_off, gemm_tiles;
   // device
@@ -108,6 +110,7 @@ struct DcPlan {
   float* Zf[2] = {nullptr, nullptr};
   float* Mbf = nullptr;
   DgemmDescT<float>* fdescs_dev = nullptr;
+  int* tc_err = nullptr;  // run_single: merges of large nodes on the tensor cores (timeout flag) when set
 
   static size_t workspace_doubles(int n);
   int build(int n);
@@ -130,14 +133,20 @@ struct DcPlan {
 // real off-diagonal |e_k| and unit quaternions phi_k = (alpha_k, beta_k)
 int phase_reduce(const double* e, int n, double* offd, double* phi, cudaStream_t st);
 // X = [diag(alpha); diag(beta)] (2n x n complex, ld), then Q X by blocked reflectors
+// tc_err (FP32 only, may be null): with it, the large products run on the
+// tensor cores (zq_tc32.cu) and a pipeline-wait timeout raises *tc_err
 template <typename R>
 int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, int64_t ldx,
-           int nbq, void* ws, cudaStream_t st);
+           int nbq, void* ws, cudaStream_t st, int* tc_err = nullptr);
 size_t form_q_workspace_bytes(int n, int nbq);
 // out (2n x n complex, ldo) = X (2n x n complex, ldx) * Z (n x n real, ldz)
 template <typename R>
 int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<R>* out, int64_t ldo,
-            DgemmDescT<R>* dev_desc, cudaStream_t st);
+            DgemmDescT<R>* dev_desc, cudaStream_t st, int* tc_err = nullptr);
+// FP32 products of the refined path's decomposition on the tensor cores or the
+// CUDA cores, per use (environment ZQ_FP32_PRODUCTS=cuda, ZQ_TC32_USES)
+enum { TC_USE_TRAIL = 0, TC_USE_FORMQ = 1, TC_USE_APPLYZ = 2, TC_USE_DC = 3 };
+bool fp32_products_on_tensor_cores(int use);
 // right half of the n2 x n2 output from the left half (U; V)
 int symmetry_fill(double2* D, int64_t ld, int n, cudaStream_t st);
 
@@ -179,6 +188,8 @@ size_t ozaki_workspace_bytes(int n);
 // (<= 0: the default, about 2 s); a test hook for the timeout path
 void set_pipeline_wait_cycles(long long cycles);
 long long pipeline_wait_cycles();
+// the driver's cuTensorMapEncodeTiled (null when unavailable)
+void* tensor_map_encode_fn();
 // upper triangle of a square structured matrix from its lower triangle (sym +1 Hermitian, -1 antisymmetric)
 int structured_fill(double2* C, int64_t ldc, int n, int sym, cudaStream_t st);
 

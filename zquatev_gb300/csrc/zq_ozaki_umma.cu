@@ -335,16 +335,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static std::once_flag once;
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
+  return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encode_fn());
 }
 
 // rows x Kp bf16, row-major (Kp contiguous); boxes of 64 K x 128 rows, 128-byte swizzle
@@ -365,6 +356,19 @@ int make_map(CUtensorMap* tm, const __nv_bfloat16* base, int64_t Kp, int64_t row
 std::atomic<long long> g_wait_cycles{UM_WAIT_CYCLES};
 
 }  // namespace
+
+void* tensor_map_encode_fn() {
+  static std::once_flag once;
+  static void* fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = p;
+  });
+  return fn;
+}
 
 int oz_umma_smem_bytes() { return UM_SMEM; }
 

@@ -431,6 +431,7 @@ size_t refine_workspace_bytes(int n, int nbq) {
   b += form_q_workspace_bytes(n, nbq);  // sized for double2, enough for float2
   b += sizeof(double) * (46 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64);
   b += sizeof(int) * (size_t)n;
+  b += 256;                             // tensor-core pipeline timeout flag
   b += 64 * 256;
   return b;
 }
@@ -588,6 +589,7 @@ int refined_solve(RefineArgs& ra) {
   void* fq_ws = take(form_q_workspace_bytes(n, ra.nbq));
   double* sm = reinterpret_cast<double*>(take(sizeof(double) * (46 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64)));
   int* rank = reinterpret_cast<int*>(take(sizeof(int) * (size_t)n));
+  int* tc_err = reinterpret_cast<int*>(take(256));
   double* d = sm; sm += n;
   double* e = sm; sm += 4 * (size_t)n;
   double* tau = sm; sm += n;
@@ -617,7 +619,9 @@ int refined_solve(RefineArgs& ra) {
                             cudaMemcpyDeviceToDevice, st));
   k_c128_to_c64<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(H0, n2, Mf, n2, n2, n);
   ZQ_LAUNCH_CHECK();
+  ZQ_CUDA(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
   TridiagView<float> vf = tridiag_bind<float>(tri_ws, Mf, n, n2, 64, d, e, tau);
+  vf.tc_err = tc_err;  // tensor-core products where fp32_products_on_tensor_cores allows them
   if (int rc = tridiagonalize<float>(vf, ra.nb, st)) return rc;
   if (int rc = phase_reduce(e, n, offd, phi, st)) return rc;
   mark(1, st);
@@ -625,16 +629,29 @@ int refined_solve(RefineArgs& ra) {
   // Q Phi (FP32) on the second stream while the divide and conquer runs
   ZQ_CUDA(cudaEventRecord(ra.ev_fork, st));
   ZQ_CUDA(cudaStreamWaitEvent(ra.st2, ra.ev_fork, 0));
-  if (int rc = form_q<float>(Mf, n2, n, phi, XfQ, n2, ra.nbq, fq_ws, ra.st2)) return rc;
+  if (int rc = form_q<float>(Mf, n2, n, phi, XfQ, n2, ra.nbq, fq_ws, ra.st2, tc_err)) return rc;
   mark(2, ra.st2);
   ZQ_CUDA(cudaEventRecord(ra.ev_join, ra.st2));
   float* Zf = nullptr;  // FP32 divide and conquer: Z in the plan's workspace
-  if (int rc = ra.dc->run_single(d, offd, lam, Zf, st)) return rc;
+  ra.dc->tc_err = tc_err;
+  const int dc_rc = ra.dc->run_single(d, offd, lam, Zf, st);
+  ra.dc->tc_err = nullptr;
+  if (dc_rc) return dc_rc;
   mark(3, st);
   ZQ_CUDA(cudaStreamWaitEvent(st, ra.ev_join, 0));
-  if (int rc = apply_z<float>(XfQ, n2, Zf, n, n, Mf, n2, ra.fdesc, st)) return rc;
+  if (int rc = apply_z<float>(XfQ, n2, Zf, n, n, Mf, n2, ra.fdesc, st, tc_err)) return rc;
   k_c64_to_c128<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(Mf, n2, X, ldd, n2, n);
   ZQ_LAUNCH_CHECK();
+  {
+    // a tensor-core pipeline wait that ran out leaves X0 unusable: report it
+    int herr = 0;
+    ZQ_CUDA(cudaMemcpyAsync(&herr, tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ZQ_CUDA(cudaStreamSynchronize(st));
+    if (herr) {
+      set_error_message("k_tc32: a pipeline wait ran out of time (kernel stopped)");
+      return ZQ_ERR_TIMEOUT;
+    }
+  }
   mark(4, st);
 
   // B. refinement

@@ -25,8 +25,11 @@
 //       gemm     - Z_node = blockdiag(Z1, Z2) * M  (grouped DGEMM).
 #include "zq_common.cuh"
 #include "zq_kernels.h"
+#include "zq_tc32.h"
 
 #include <algorithm>
+#include <atomic>
+#include <type_traits>
 #include <vector>
 
 namespace zq {
@@ -398,17 +401,20 @@ int DcPlan::build(int n_) {
   }
   max_depth = depth - 1;
   // group by depth: internal nodes and leaves separately, each sorted by a
+  depth_mmax.clear();
   for (int t = 0; t <= max_depth; ++t) {
     depth_off.push_back((int)nodes_host.size());
-    int cnt = 0;
+    int cnt = 0, mmax = 0;
     for (auto& x : all)
       if (x.depth == t && x.b - x.a > 1) {
         DcNode nd{};
         nd.a = x.a; nd.b = x.b; nd.c = x.a + (x.b - x.a) / 2;
         nodes_host.push_back(nd);
         ++cnt;
+        mmax = std::max(mmax, x.b - x.a);
       }
     depth_cnt.push_back(cnt);
+    depth_mmax.push_back(mmax);
   }
   for (int t = 0; t <= max_depth; ++t) {
     leaf_off.push_back((int)nodes_host.size());
@@ -552,8 +558,30 @@ static int dc_run(DcPlan& P, const double* d, const double* e, double* lam_out, 
     k_dc_rotate<ZT><<<ceil_div(n, 128), 128, 0, st>>>(nd, cnt, P.w, Mb, n);
     ZQ_LAUNCH_CHECK();
     if (P.gemm_tiles[t] > 0) {
-      grouped_launch<ZT>(descs + P.gemm_off[t], 2 * cnt, P.gemm_tiles[t], st);
-      ZQ_LAUNCH_CHECK();
+      bool done = false;
+      if constexpr (std::is_same<ZT, float>::value) {
+        // FP32 merges of large nodes on the tensor cores (TF32 x3), one product per child
+        if (P.tc_err && P.depth_mmax[t] >= 512 && fp32_products_on_tensor_cores(TC_USE_DC)) {
+          for (int q = 0; q < 2 * cnt; ++q) {
+            const DgemmDesc& h = P.gemm_host[P.gemm_off[t] + q];
+            Tc32Args g{};
+            g.cplx = 0; g.m = h.m; g.n = h.n; g.nseg = 1;
+            g.seg[0].a.p = Zi + h.off_a; g.seg[0].a.ld = h.lda; g.seg[0].a.kfast = 0; g.seg[0].a.sign = 1.f;
+            g.seg[0].b.p = Mb + h.off_b; g.seg[0].b.ld = h.ldb; g.seg[0].b.kfast = 1; g.seg[0].b.sign = 1.f;
+            g.seg[0].k = h.k;
+            g.alpha = make_float2(1.f, 0.f); g.beta = make_float2(0.f, 0.f);
+            g.C = Zo + h.off_c; g.ldc = h.ldc;
+            g.splits = 1;
+            g.err = P.tc_err;
+            if (int rc = tc32_gemm(g, st)) return rc;
+          }
+          done = true;
+        }
+      }
+      if (!done) {
+        grouped_launch<ZT>(descs + P.gemm_off[t], 2 * cnt, P.gemm_tiles[t], st);
+        ZQ_LAUNCH_CHECK();
+      }
     }
   }
   k_dc_unscale<<<ceil_div(n, 256), 256, 0, st>>>(P.lam[0], n, P.scal);

@@ -46,6 +46,12 @@
 // and reflector scalars are still formed in double.
 #include "zq_common.cuh"
 #include "zq_kernels.h"
+#include "zq_tc32.h"
+
+#include <cuda.h>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
 
 namespace zq {
 
@@ -742,6 +748,56 @@ __global__ void __launch_bounds__(NT) k_trail(TridiagView<R> v, int p, int nbp, 
   }
 }
 
+// The same trailing update on the tensor cores (zq_tc32.cu), FP32 path, used
+// only where ZQ_TC32_USES names it: the lower triangles of the (n - t0)^2
+// trailing blocks of A and B take one rank-4 nbp product each,
+//   A -= [Wa | conj(Wb) | Ya | conj(Yb)] [conj(Ya) | Yb | conj(Wa) | Wb]^T   (i >= j)
+//   B -= [Wb | -conj(Wa) | Yb | -conj(Ya)] [conj(Ya) | Yb | conj(Wa) | Wb]^T (i > j)
+// with W the panel's reflectors (stored in place, columns p..p+nbp-1) and Y
+// its aux vectors, all read at rows t0.. (128 x 128 lower tiles only).
+static Tc32Src trail_src(const float2* p, int64_t ld, int conj, float sign) {
+  Tc32Src s{};
+  s.p = reinterpret_cast<const float*>(p); s.ld = ld; s.kfast = 0; s.conj = conj; s.sign = sign;
+  return s;
+}
+static int trail_tc32(const TridiagView<float>& v, int p, int nbp, int t0, cudaStream_t st) {
+  const int n = v.n;
+  const int64_t ld = v.ld;
+  const float2* Wa = v.M + t0 + (int64_t)p * ld;
+  const float2* Wb = v.M + n + t0 + (int64_t)p * ld;
+  const float2* Ya = v.Ya + t0;
+  const float2* Yb = v.Yb + t0;
+  for (int half = 0; half < 2; ++half) {
+    Tc32Args t{};
+    t.cplx = 1; t.m = n - t0; t.n = n - t0; t.nseg = 4;
+    // column operand, shared by both updates
+    t.seg[0].b = trail_src(Ya, v.ldy, 1, 1.f);
+    t.seg[1].b = trail_src(Yb, v.ldy, 0, 1.f);
+    t.seg[2].b = trail_src(Wa, ld, 1, 1.f);
+    t.seg[3].b = trail_src(Wb, ld, 0, 1.f);
+    if (half == 0) {
+      t.seg[0].a = trail_src(Wa, ld, 0, 1.f);
+      t.seg[1].a = trail_src(Wb, ld, 1, 1.f);
+      t.seg[2].a = trail_src(Ya, v.ldy, 0, 1.f);
+      t.seg[3].a = trail_src(Yb, v.ldy, 1, 1.f);
+    } else {
+      t.seg[0].a = trail_src(Wb, ld, 0, 1.f);
+      t.seg[1].a = trail_src(Wa, ld, 1, -1.f);
+      t.seg[2].a = trail_src(Yb, v.ldy, 0, 1.f);
+      t.seg[3].a = trail_src(Ya, v.ldy, 1, -1.f);
+    }
+    for (int q = 0; q < 4; ++q) t.seg[q].k = nbp;
+    t.alpha = make_float2(-1.f, 0.f); t.beta = make_float2(1.f, 0.f);
+    t.C = reinterpret_cast<float*>(v.M + (half ? n : 0) + t0 + (int64_t)t0 * ld);
+    t.ldc = ld;
+    t.tri = half ? 2 : 1;
+    t.splits = 1;
+    t.err = v.tc_err;
+    if (int rc = tc32_gemm(t, st)) return rc;
+  }
+  return ZQ_OK;
+}
+
 // ----------------------------------------------------------------------------
 // host driver
 // ----------------------------------------------------------------------------
@@ -790,6 +846,14 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
       prof_end(PC_PANEL, st);
       const int nblk = ceil_div(n - t0, TB);
       prof_begin(PC_TRAIL, st);
+      if constexpr (std::is_same<R, float>::value) {
+        if (v.tc_err && fp32_products_on_tensor_cores(TC_USE_TRAIL)) {
+          if (int rc = trail_tc32(v, p, nbp, t0, st)) return rc;
+          prof_end(PC_TRAIL, st);
+          ncp = 0;
+          continue;
+        }
+      }
       ZQ_CUDA(launch_pdl(k_trail<R>, dim3(nblk * (nblk + 1) / 2), dim3(NT), st, v, p, nbp, t0));
       count_launch();
       prof_end(PC_TRAIL, st);

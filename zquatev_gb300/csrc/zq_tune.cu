@@ -14,6 +14,8 @@
 #include "zq_common.cuh"
 #include "zq_context.h"
 #include "zq_kernels.h"
+
+#include <type_traits>
 #include "../../include/zquatev_gb300.h"
 
 #include <algorithm>
@@ -55,7 +57,7 @@ int tune_nb(int n, const int* cand, int ncand, double* ms_out, int* best, cudaSt
   const size_t wbytes = tridiag_workspace_bytes<R>(n, 64);
   const size_t sbytes = sizeof(double) * (size_t)(6 * n + 16);
   void* mem = nullptr;
-  ZQ_CUDA(cudaMallocAsync(&mem, mbytes + wbytes + sbytes + 1024, st));
+  ZQ_CUDA(cudaMallocAsync(&mem, mbytes + wbytes + sbytes + 1024 + 256, st));
   char* p = reinterpret_cast<char*>(mem);
   cplx<R>* M = reinterpret_cast<cplx<R>*>(p);
   void* ws = p + ((mbytes + 255) & ~(size_t)255);
@@ -64,6 +66,12 @@ int tune_nb(int n, const int* cand, int ncand, double* ms_out, int* best, cudaSt
   double* e = sm + n;
   double* tau = sm + 5 * (size_t)n;
   TridiagView<R> v = tridiag_bind<R>(ws, M, n, 2 * n, 64, d, e, tau);
+  if (std::is_same<R, float>::value) {
+    // time the FP32 reduction as the refined path runs it
+    v.tc_err = reinterpret_cast<int*>(p + ((mbytes + 255) & ~(size_t)255) + ((wbytes + 255) & ~(size_t)255) +
+                                      ((sbytes + 255) & ~(size_t)255));
+    ZQ_CUDA(cudaMemsetAsync(v.tc_err, 0, sizeof(int), st));
+  }
   cudaEvent_t e0, e1;
   ZQ_CUDA(cudaEventCreate(&e0));
   ZQ_CUDA(cudaEventCreate(&e1));
