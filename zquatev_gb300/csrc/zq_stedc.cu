@@ -56,16 +56,31 @@ __global__ void k_dc_leaf(const DcNode* nodes, int cnt, const double* dmod, ZT* 
   lamout[a] = dmod[a];
 }
 
-// one CTA per internal node
+// one CTA per internal node. The merged poles (value, z, source column) are
+// staged in shared memory when the node fits (m <= scap): the deflation scan
+// is sequential (each close-pole rotation changes the next comparison) and
+// runs in one thread, so its operands must be a shared-memory load away, not
+// an L2 round trip. The scales are block reductions; the deflated list is
+// ranked from shared memory.
+constexpr int DC_SCAP = 8192;  // largest node staged in shared memory (20 bytes per pole)
 template <typename ZT>
-__global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, const ZT* Zin, const double* lamin, int n) {
+__global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, const ZT* Zin, const double* lamin, int n,
+                                                    int scap) {
+  extern __shared__ double dc_sm[];
   DcNode& nd = nodes[blockIdx.x];
   const int a = nd.a, c = nd.c, b = nd.b;
   const int m = b - a, n1 = c - a, n2 = b - c;
   const int tid = threadIdx.x;
   const double rho2 = 2.0 * nd.rho;
   const double rs2 = 0.70710678118654752440;
+  const bool staged = m <= scap;
+  double* D = staged ? dc_sm : w.sd + a;
+  double* Zs = staged ? dc_sm + scap : w.sz + a;
+  int* P = staged ? reinterpret_cast<int*>(dc_sm + 2 * scap) : w.perm + a;
+  __shared__ double s_red[8];
+  __shared__ int s_cnt[3];
   // merge the two sorted eigenvalue lists; z in sorted order
+  double dm = 0.0, zm = 0.0;
   for (int i = tid; i < m; i += blockDim.x) {
     double val, z;
     int pos;
@@ -84,21 +99,18 @@ __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, con
       while (lo < hi) { const int mid = (lo + hi) >> 1; if (lamin[a + mid] <= val) lo = mid + 1; else hi = mid; }
       pos = i2 + lo;
     }
-    w.sd[a + pos] = val;
-    w.sz[a + pos] = z;
-    w.perm[a + pos] = i;
+    D[pos] = val;
+    Zs[pos] = z;
+    P[pos] = i;
+    dm = fmax(dm, fabs(val));
+    zm = fmax(zm, fabs(z));
   }
-  __syncthreads();
-  __shared__ int s_cnt[3];
+  const double dmax = block_max(dm, s_red);  // (its barriers also publish D, Zs, P)
+  const double zmax = block_max(zm, s_red);
   if (tid == 0) {
-    double dmax = 0.0, zmax = 0.0;
-    for (int i = 0; i < m; ++i) { dmax = fmax(dmax, fabs(w.sd[a + i])); zmax = fmax(zmax, fabs(w.sz[a + i])); }
     const double tol = 8.0 * DEPS * fmax(dmax, zmax);
     int K = 0, nd_ = 0, nr = 0;
     int pj = -1;
-    double* D = w.sd + a;
-    double* Zs = w.sz + a;
-    const int* P = w.perm + a;
     for (int j = 0; j < m; ++j) {
       if (rho2 * fabs(Zs[j]) <= tol) {
         w.df_val[a + nd_] = D[j]; w.df_col[a + nd_] = P[j]; ++nd_;
@@ -130,11 +142,17 @@ __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, con
   __syncthreads();
   // sort the deflated list (values, columns) by rank; ties by index
   const int nd_ = s_cnt[0];
+  const double* fv = w.df_val + a;
+  if (staged) {  // the staged poles are dead now: their space holds the deflated values
+    for (int i = tid; i < nd_; i += blockDim.x) dc_sm[i] = w.df_val[a + i];
+    __syncthreads();
+    fv = dc_sm;
+  }
   for (int i = tid; i < nd_; i += blockDim.x) {
-    const double v = w.df_val[a + i];
+    const double v = fv[i];
     int rank = 0;
     for (int l = 0; l < nd_; ++l) {
-      const double u = w.df_val[a + l];
+      const double u = fv[l];
       rank += (u < v) || (u == v && l < i);
     }
     w.df_sval[a + rank] = v;
@@ -547,8 +565,23 @@ static int dc_run(DcPlan& P, const double* d, const double* e, double* lam_out, 
     const int cnt = P.depth_cnt[t];
     if (cnt == 0) continue;
     DcNode* nd = P.nodes_dev + P.depth_off[t];
-    k_dc_prepare<ZT><<<cnt, 256, 0, st>>>(nd, P.w, Zi, li, n);
-    ZQ_LAUNCH_CHECK();
+    {
+      // shared-memory staging of the merged poles for the depth's largest node
+      const int scap = P.depth_mmax[t] <= DC_SCAP ? P.depth_mmax[t] : 0;
+      const size_t smem = (size_t)scap * 20;
+      if (smem > 48 * 1024) {
+        static std::atomic<unsigned long long> attr_set{0};
+        int dev = 0;
+        ZQ_CUDA(cudaGetDevice(&dev));
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(attr_set.load() & bit)) {
+          ZQ_CUDA(cudaFuncSetAttribute(k_dc_prepare<ZT>, cudaFuncAttributeMaxDynamicSharedMemorySize, DC_SCAP * 20));
+          attr_set.fetch_or(bit);
+        }
+      }
+      k_dc_prepare<ZT><<<cnt, 256, smem, st>>>(nd, P.w, Zi, li, n, scap);
+      ZQ_LAUNCH_CHECK();
+    }
     k_dc_secular<<<ceil_div(n, 4), 128, 0, st>>>(nd, cnt, P.w);
     ZQ_LAUNCH_CHECK();
     k_dc_zhat<<<ceil_div(n, 4), 128, 0, st>>>(nd, cnt, P.w);

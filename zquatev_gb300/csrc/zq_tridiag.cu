@@ -545,6 +545,181 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int p, int j, in
 }
 
 // ----------------------------------------------------------------------------
+// hemv, FP32 with TMA staging (even n): the same products and partial layout
+// as k_hemv, but
+//   * the A and B tiles arrive by cp.async.bulk.tensor: each 32 x 32 complex
+//     tile is two 16-row boxes (128 bytes of rows, 128-byte swizzle, zeros
+//     outside the matrix) issued by one thread, completed on an mbarrier;
+//   * the tile grid starts at the even row b0 = r0 - (r0 & 1), as a TMA box
+//     must start on a 16-byte boundary; row / column b0 < r0 carries w = 0 and
+//     its output is not read (k_hreduce is told the shift);
+//   * a complex multiply-add m v is two packed FP32 FMAs on the natural pair
+//     (m.x, m.y): P += (m.x, m.y) (v.x, v.x), Q += (m.x, m.y) (v.y, v.y), and
+//     m v = (P.x - Q.y, P.y + Q.x), conj(m) v = (P.x + Q.y, Q.x - P.y), so the
+//     vectors are kept in shared memory as (v.x, v.x, v.y, v.y).
+// Warp roles as k_hemv: 0 A rows, 1 B rows, 2 A^H columns, 3 -B^T columns.
+// ----------------------------------------------------------------------------
+constexpr int HM_SMEM = 16384 + 1024;  // two tiles (8 KB each) + alignment
+__device__ __forceinline__ void fma2(float2& acc, float2 a, float2 b) {
+  asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%0, %1};\n\t"
+      "fma.rn.f32x2 rc, ra, rb, rc;\n\tmov.b64 {%0, %1}, rc;\n\t}"
+      : "+f"(acc.x), "+f"(acc.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+}
+__device__ __forceinline__ float2 lds2(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a));
+  return v;
+}
+
+__global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtensorMap tm, TridiagView<float> v, int p,
+                                                  int j, int k, int ndot, int b0) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+  using Z = float2;
+  extern __shared__ __align__(1024) unsigned char hm_raw[];
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(hm_raw);
+  const uint32_t tiles = (raw + 1023u) & ~1023u;    // A tile at +0, B tile at +8192
+  unsigned char* tiles_gen = hm_raw + (tiles - raw);
+  __shared__ float4 s_xd[2][HT], s_zd[2][HT];       // [0]: block I rows, [1]: block J rows
+  __shared__ Z sout[HT][4];
+  __shared__ __align__(8) unsigned long long s_bar;
+  const int n = v.n;
+  const int64_t ld = v.ld;
+  const Z* A = v.M;
+  const Z* B = v.M + n;
+  if ((int)blockIdx.x < ndot) {
+    panel_dots(v, p, j, k, blockIdx.x, ndot, reinterpret_cast<Z*>(tiles_gen));
+    return;
+  }
+  const int t = blockIdx.x - ndot;
+  int I, J;
+  tri_tile(t, I, J);
+  const bool diag = (I == J);
+  const int tid = threadIdx.x;
+  const int rbase = b0 + I * HT, cbase = b0 + J * HT;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(16384u) : "memory");
+    const uint64_t tma = reinterpret_cast<uint64_t>(&tm);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int x = (q >= 2 ? n : 0) + rbase + 16 * (q & 1);   // row: even (b0, n even)
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+              tiles + 4096u * q),
+          "l"(tma), "r"(x), "r"(cbase), "r"(bar)
+          : "memory");
+    }
+  }
+  // meanwhile: w on the rows of block I (column products) and block J (row products)
+  if (tid < 2 * HT) {
+    const int ws = tid >> 5, wq = tid & (HT - 1);
+    const int wg = (ws == 0 ? rbase : cbase) + wq;
+    Z x = czero<Z>(), z = czero<Z>();
+    if (wg > j && wg < n) {
+      WHead<float> h;
+      load_head(v, h);
+      x = A[wg + (int64_t)j * ld];
+      z = B[wg + (int64_t)j * ld];
+      w_from_x<float>(h, wg, j, x, z);
+      z = cconj(z);
+    }
+    s_xd[ws][wq] = make_float4(x.x, x.x, x.y, x.y);
+    s_zd[ws][wq] = make_float4(z.x, z.x, z.y, z.y);
+  }
+  __syncthreads();
+  {
+    // bounded wait for the tiles (the copies take microseconds)
+    const long long t0 = clock64();
+    uint32_t ok = 0;
+    while (!ok) {
+      asm volatile(
+          "{\n\t.reg .pred pp;\n\tmbarrier.try_wait.parity.shared::cta.b64 pp, [%1], 0;\n\tselp.u32 %0, 1, 0, pp;\n\t}"
+          : "=r"(ok)
+          : "r"(bar)
+          : "memory");
+      if (!ok && clock64() - t0 > 4000000000LL) break;
+    }
+    if (!__all_sync(0xffffffffu, ok != 0)) {
+      if ((tid & 31) == 0 && v.tc_err) atomicExch(v.tc_err, 1);
+      return;
+    }
+  }
+  const int role = tid >> 5, q = tid & (HT - 1);
+  Z P0 = czero<Z>(), Q0 = czero<Z>(), P1 = czero<Z>(), Q1 = czero<Z>();
+  if (role < 2) {
+    // row q of the tile, all 32 columns: element (q, c) of a swizzled 16-row box
+    // sits at box * 4096 + c * 128 + (((q & 15) >> 1) ^ (c & 7)) * 16 + (q & 1) * 8
+    const uint32_t rowb = tiles + (uint32_t)role * 8192u + (uint32_t)(q >> 4) * 4096u + (uint32_t)(q & 1) * 8u;
+    const int hr = (q & 15) >> 1;
+    if (!diag) {
+#pragma unroll
+      for (int c = 0; c < HT; ++c) {
+        const float2 m = lds2(rowb + (uint32_t)c * 128u + (uint32_t)((hr ^ (c & 7)) << 4));
+        const float4 xd = s_xd[1][c], zd = s_zd[1][c];
+        fma2(P0, m, make_float2(xd.x, xd.y)); fma2(Q0, m, make_float2(xd.z, xd.w));
+        fma2(P1, m, make_float2(zd.x, zd.y)); fma2(Q1, m, make_float2(zd.z, zd.w));
+      }
+    } else {
+      for (int c = 0; c <= q; ++c) {
+        float2 m = lds2(rowb + (uint32_t)c * 128u + (uint32_t)((hr ^ (c & 7)) << 4));
+        if (c == q) { if (role == 0) m.y = 0.f; else m = czero<Z>(); }  // real diagonal of A, zero of B
+        const float4 xd = s_xd[1][c], zd = s_zd[1][c];
+        fma2(P0, m, make_float2(xd.x, xd.y)); fma2(Q0, m, make_float2(xd.z, xd.w));
+        fma2(P1, m, make_float2(zd.x, zd.y)); fma2(Q1, m, make_float2(zd.z, zd.w));
+      }
+    }
+  } else {
+    // column q, all 32 rows r: element (r, q) at (r >> 4) * 4096 + q * 128 + (((r & 15) >> 1) ^ (q & 7)) * 16 + (r & 1) * 8
+    const uint32_t colb = tiles + (uint32_t)(role - 2) * 8192u + (uint32_t)q * 128u;
+    const int hq = q & 7;
+    if (!diag) {
+#pragma unroll
+      for (int r = 0; r < HT; ++r) {
+        const float2 m = lds2(colb + (uint32_t)(r >> 4) * 4096u + (uint32_t)((((r & 15) >> 1) ^ hq) << 4) + (uint32_t)(r & 1) * 8u);
+        const float4 xd = s_xd[0][r], zd = s_zd[0][r];
+        fma2(P0, m, make_float2(xd.x, xd.y)); fma2(Q0, m, make_float2(xd.z, xd.w));
+        fma2(P1, m, make_float2(zd.x, zd.y)); fma2(Q1, m, make_float2(zd.z, zd.w));
+      }
+    } else {
+      for (int r = q + 1; r < HT; ++r) {  // diagonal tile: strictly below the diagonal
+        const float2 m = lds2(colb + (uint32_t)(r >> 4) * 4096u + (uint32_t)((((r & 15) >> 1) ^ hq) << 4) + (uint32_t)(r & 1) * 8u);
+        const float4 xd = s_xd[0][r], zd = s_zd[0][r];
+        fma2(P0, m, make_float2(xd.x, xd.y)); fma2(Q0, m, make_float2(xd.z, xd.w));
+        fma2(P1, m, make_float2(zd.x, zd.y)); fma2(Q1, m, make_float2(zd.z, zd.w));
+      }
+    }
+  }
+  // this warp's two products
+  Z u0, u1;
+  if (role < 2) {            // m v
+    u0 = mk(P0.x - Q0.y, P0.y + Q0.x); u1 = mk(P1.x - Q1.y, P1.y + Q1.x);
+  } else if (role == 2) {    // conj(m) v
+    u0 = mk(P0.x + Q0.y, Q0.x - P0.y); u1 = mk(P1.x + Q1.y, Q1.x - P1.y);
+  } else {                   // -m v
+    u0 = mk(Q0.y - P0.x, -(P0.y + Q0.x)); u1 = mk(Q1.y - P1.x, -(P1.y + Q1.x));
+  }
+  const int nbm = v.hblk;
+  if (role >= 2) {
+    if (diag) { sout[q][2 * (role - 2)] = u0; sout[q][2 * (role - 2) + 1] = u1; }
+    else {
+      Z* o = v.hpart + (((int64_t)J * nbm + I) * HT + q) * 4 + 2 * (role - 2);
+      o[0] = u0; o[1] = u1;
+    }
+  }
+  if (diag) __syncthreads();
+  if (role < 2) {
+    Z a0 = u0, a1 = u1;
+    if (diag) { a0 = cadd(a0, sout[q][2 * role]); a1 = cadd(a1, sout[q][2 * role + 1]); }
+    Z* o = v.hpart + (((int64_t)I * nbm + J) * HT + q) * 4 + 2 * role;
+    o[0] = a0; o[1] = a1;
+  }
+}
+
+// ----------------------------------------------------------------------------
 // hreduce: g = H_panelstart w - corrections, for rows [j+1, n); c partials;
 //   w = f x written in place of x.
 //   T is the hemv tile edge used for this column; nblk its number of blocks.
@@ -557,7 +732,8 @@ constexpr int HRB = 8;                 // rows per CTA
 constexpr int HNG = NT / HRB;          // reflector groups for the corrections
 constexpr int NSPL = NT / (4 * HRB);   // threads per (row, product) for the tile partials
 template <typename R>
-__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode) {
+__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode,
+                                                int sh) {
   pdl_wait();  // launched with launch_pdl: the previous kernel's results first
   using Z = cplx<R>;
   const int n = v.n;
@@ -594,7 +770,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
     const int lr = blockIdx.x * HRB + (o >> 2);
     Z s0 = czero<Z>(), s1 = czero<Z>(), s2 = czero<Z>(), s3 = czero<Z>();
     if (r0 + lr < n) {
-      const int Rb = lr / T, off = lr % T;
+      const int Rb = (lr + sh) / T, off = (lr + sh) % T;  // the hemv tile grid starts sh rows above r0
       const Z* base = v.hpart + (((int64_t)Rb * v.hblk) * T + off) * 4 + (o & 3);
       const int64_t stride = (int64_t)T * 4;
       int S = sp;
@@ -748,6 +924,16 @@ __global__ void __launch_bounds__(NT) k_trail(TridiagView<R> v, int p, int nbp, 
   }
 }
 
+// TMA-staged FP32 hemv on (default) or the register-staged k_hemv (environment
+// ZQ_HEMV=ldg)
+static bool hemv_tma_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("ZQ_HEMV");
+    return !(e && !strcmp(e, "ldg"));
+  }();
+  return on;
+}
+
 // The same trailing update on the tensor cores (zq_tc32.cu), FP32 path, used
 // only where ZQ_TC32_USES names it: the lower triangles of the (n - t0)^2
 // trailing blocks of A and B take one rank-4 nbp product each,
@@ -808,6 +994,24 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
   if (nb > v.nbmax) nb = v.nbmax;
   if (nb < 1) nb = 1;
   ZQ_CUDA(cudaMemsetAsync(v.counter, 0, 2 * sizeof(unsigned), st));
+  // FP32 with even n: the hemv tiles come by TMA from one tensor map over [A; B]
+  // (2n x n, 8-byte elements, 16 x 32 boxes, 128-byte swizzle, zeros outside)
+  bool use_tma = false;
+  CUtensorMap hemv_map;
+  if (std::is_same<R, float>::value && (n % 2) == 0 && n >= 4 && hemv_tma_enabled()) {
+    using Enc = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                             const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                             CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    auto enc = reinterpret_cast<Enc>(tensor_map_encode_fn());
+    const cuuint64_t dims[2] = {(cuuint64_t)2 * n, (cuuint64_t)n};
+    const cuuint64_t strides[1] = {(cuuint64_t)v.ld * 8};
+    const cuuint32_t box[2] = {16u, (cuuint32_t)HT};
+    const cuuint32_t es[2] = {1u, 1u};
+    use_tma = enc && (reinterpret_cast<uintptr_t>(v.M) % 16) == 0 && (v.ld % 2) == 0 &&
+              enc(&hemv_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void*>(reinterpret_cast<const void*>(v.M)),
+                  dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
   int ncp = 0;  // number of c partials of the previous column
   for (int p = 0; p < n; p += nb) {
     const int nbp = (nb < n - p) ? nb : (n - p);
@@ -820,19 +1024,30 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
       count_launch();
       if (L < 1) { prof_end(PC_PANEL, st); ncp = 0; continue; }
       const int T = HT;
-      const int nblk = ceil_div(L, T);
+      // TMA-staged FP32 hemv: its tile grid starts at the even row below r0
+      const int b0 = use_tma ? ((j + 1) & ~1) : (j + 1);
+      const int sh = (j + 1) - b0;
+      const int nblk = ceil_div(n - b0, T);
       const int ndot = (k > 0 && L >= 2) ? ceil_div(L, DR) : 0;  // dot-partial CTAs of the hemv grid
       prof_end(PC_PANEL, st);
       if (L >= 2) {
         prof_begin(PC_HEMV, st);
         const int ntiles = nblk * (nblk + 1) / 2;
-        ZQ_CUDA(launch_pdl(k_hemv<R>, dim3(ntiles + ndot), dim3(128), st, v, p, j, k, ndot));
+        if constexpr (std::is_same<R, float>::value) {
+          if (use_tma) {
+            ZQ_CUDA(launch_pdl_smem(k_hemv_tma, dim3(ntiles + ndot), dim3(128), HM_SMEM, st, hemv_map, v, p, j, k, ndot, b0));
+          } else {
+            ZQ_CUDA(launch_pdl(k_hemv<R>, dim3(ntiles + ndot), dim3(128), st, v, p, j, k, ndot));
+          }
+        } else {
+          ZQ_CUDA(launch_pdl(k_hemv<R>, dim3(ntiles + ndot), dim3(128), st, v, p, j, k, ndot));
+        }
         count_launch();
         prof_end(PC_HEMV, st);
       }
       prof_begin(PC_PANEL, st);
       const int nhr = ceil_div(L, HRB);
-      ZQ_CUDA(launch_pdl(k_hreduce<R>, dim3(nhr), dim3(NT), st, v, p, j, k, T, nblk, L < 2 ? 1 : 0));
+      ZQ_CUDA(launch_pdl(k_hreduce<R>, dim3(nhr), dim3(NT), st, v, p, j, k, T, nblk, L < 2 ? 1 : 0, sh));
       count_launch();
       prof_end(PC_PANEL, st);
       ncp = nhr;
