@@ -101,14 +101,15 @@ int zq_zgemm_accurate(int opa, int opb, int m, int n, int k, const double* A, in
 int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig, void* stream);
 
 /* Panel width of the blocked tridiagonalisation (the reference hard-codes
- * nb = 20 at zquatev.cc:64). Valid range 1..64; default 32. */
+ * nb = 20 at zquatev.cc:64). Valid range 1..128; default 32. */
 int zq_set_block_size(int nb);
 int zq_get_block_size(void);
 
 /* Tensor-core kernel of the Ozaki products in the refined path and
  * zq_zgemm_accurate: 0 = mma.sync (bf16 m16n8k16, 64 x 64 tiles), 1 = tcgen05
- * (TMEM accumulators, TMA-fed 128 x 256 MMAs; the default). Same arithmetic
- * and results. */
+ * (TMEM accumulators, TMA-fed 128 x 256 MMAs; the default), 2 = tcgen05 in
+ * clusters of two CTAs that share the B operand by TMA multicast. Same
+ * arithmetic and results. */
 int zq_set_ozaki_kernel(int which);
 int zq_get_ozaki_kernel(void);
 
@@ -132,12 +133,12 @@ int zq_gemm_tf32x3(int cplx, int opa, int opb, int m, int n, int k, const float*
                    int ldb, float* C, int ldc, int splits, void* stream);
 
 /* Panel-width autotuner: times the quaternion tridiagonalisation of a seeded
- * random matrix of order n2 for nb in {16, 32, 64} and stores the fastest for
- * n2's size bucket (powers of two of n) and precision (0: FP64 path, 1: FP32
- * decomposition of the refined path); later solves of that bucket use it.
- * best_nb receives the choice, ms (3 doubles, may be NULL) the timings. The
- * reference hard-codes nb = 20 (zquatev.cc:64); nb = 128 is not offered (the
- * panel kernels hold at most 64 reflectors). zq_set_block_size clears the table. */
+ * random matrix of order n2 for nb in {16, 32, 64, 128} and stores the fastest
+ * for n2's size bucket (powers of two of n) and precision (0: FP64 path, 1:
+ * FP32 decomposition of the refined path); later solves of that bucket use it.
+ * best_nb receives the choice, ms (4 doubles, may be NULL) the timings. The
+ * reference hard-codes nb = 20 (zquatev.cc:64). zq_set_block_size clears the
+ * table. */
 int zq_autotune_nb(int n2, int precision, int* best_nb, double* ms);
 /* Tuned width for n2's bucket (0 = not tuned), and setting it directly (e.g.
  * from a saved table; 0 clears). */
@@ -160,6 +161,16 @@ int zq_batch_plan_run(zq_batch_plan* p, double* dD, double* deig, void* stream);
 int zq_batch_plan_info(zq_batch_plan* p, void* stream);
 /* Chosen CTAs per SM, CTAs of the captured launch, and the tuning times (4 doubles, ms; 0 = not tried). */
 int zq_batch_plan_shape(zq_batch_plan* p, int* ctas_per_sm, int* ctas, double* tune_ms);
+/* The per-size kernel variant the plan's autotuner chose: matrices of order
+ * n <= *warp_max_n are solved one per warp (eight per CTA), larger ones one per
+ * CTA, in the same persistent launch. ms (4 doubles, may be NULL): the tuning
+ * times for the switch sizes 0 (CTA variant only), 16, 24 and 32. No
+ * counterpart in the reference (one matrix per call). */
+int zq_batch_plan_variant(zq_batch_plan* p, int* warp_max_n, double* ms);
+/* Switch size of the warp variant for batched launches that are not planned
+ * (zquatev_batched_device, the request server): 0..32, or -1 for the default
+ * (24; environment ZQ_BATCH_WARP_MAX). */
+int zq_set_batch_warp_max(int n);
 int zq_batch_plan_destroy(zq_batch_plan* p);
 
 /* Kernel-class timing with CUDA events on the launching streams (for the

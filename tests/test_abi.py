@@ -60,7 +60,7 @@ def test_argument_errors(lib):
     assert lib.zquatev_c(0, None, 1, None) == 0
     assert "ld2" in _lib.last_error() or "null" in _lib.last_error() or _lib.last_error() == ""
     assert lib.zq_set_block_size(0) == -5
-    assert lib.zq_set_block_size(65) == -5
+    assert lib.zq_set_block_size(129) == -5
     assert lib.zq_set_block_size(32) == 0 and lib.zq_get_block_size() == 32
     assert lib.zq_stedc_device(-1, None, None, None, None, 1, None) == -5
     n2s = (ctypes.c_int * 1)(3)

@@ -101,13 +101,28 @@ def test_random_sizes(gpu, n):
     check_solution(d, out, eig, n)
 
 
-@pytest.mark.parametrize("nb", [1, 2, 8, 16, 32, 64])
+@pytest.mark.parametrize("nb", [1, 2, 8, 16, 32, 64, 100, 128])
 def test_panel_widths(gpu, nb):
     assert gpu.zq_set_block_size(nb) == 0
     try:
         n = 150
         d = inputs.random_matrix(n, 77)
         out, eig = run(d)
+        check_solution(d, out, eig, n)
+    finally:
+        gpu.zq_set_block_size(32)
+
+
+@pytest.mark.parametrize("nb", [16, 64, 128])
+def test_panel_widths_refined(gpu, nb):
+    """The refined path's FP32 reduction (TMA-staged hemv) at panel widths up
+    to 128, several panels deep, without the FP64 fallback."""
+    assert gpu.zq_set_block_size(nb) == 0
+    try:
+        n = 400
+        d = inputs.random_matrix(n, 79)
+        out, eig = run(d, fn=solver.zquatev_refined)
+        assert not solver.refine_stats()[2]
         check_solution(d, out, eig, n)
     finally:
         gpu.zq_set_block_size(32)

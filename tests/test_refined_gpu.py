@@ -41,7 +41,7 @@ def test_refined_random(gpu, n, mode):
     assert np.all(np.diff(eig[:n]) >= 0)
 
 
-@pytest.mark.parametrize("kernel", [0, 1], ids=["mma_sync", "tcgen05"])
+@pytest.mark.parametrize("kernel", [0, 1, 2], ids=["mma_sync", "tcgen05", "tcgen05_multicast"])
 @pytest.mark.parametrize("opa,opb,m,n,k", [(2, 0, 70, 50, 300), (1, 0, 70, 50, 300), (0, 0, 70, 50, 300),
                                            (0, 3, 70, 50, 300), (0, 0, 128, 128, 32), (2, 0, 300, 260, 700)])
 def test_accurate_zgemm(gpu, kernel, opa, opb, m, n, k):
@@ -72,6 +72,26 @@ def test_accurate_zgemm(gpu, kernel, opa, opb, m, n, k):
     scale = np.abs(op(a, opa)) @ np.abs(op(b, opb))
     err = np.abs(c - exact.astype(np.complex128)) / scale
     assert err.max() < 2e-15
+
+
+@pytest.mark.parametrize("n", [64, 300, 700])
+def test_refined_multicast_products(gpu, n):
+    """The refined path with its Ozaki products on the two-CTA multicast
+    kernel (lower-triangle and full-tile launches, odd tile counts that leave a
+    tile past the matrix in the last cluster) meets the same bar."""
+    assert gpu.zq_set_ozaki_kernel(2) == 0
+    try:
+        d = inputs.random_matrix(n, 6300 + n)
+        out, eig = refined(gpu, d, 1)
+    finally:
+        gpu.zq_set_ozaki_kernel(1)
+    h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
+    ref = np.linalg.eigvalsh(h)[::2]
+    hn = metrics.h_norm2(ref)
+    assert metrics.eig_error(eig[:n], ref, hn) <= TOL
+    assert metrics.residual(h, out, eig[:n]) <= TOL
+    assert metrics.orthonormality(out) <= TOL
+    assert metrics.structure_exact(out, n)
 
 
 @pytest.fixture

@@ -11,8 +11,8 @@ pytestmark = pytest.mark.gpu
 def test_autotune_nb(gpu, precision):
     best, ms = solver.autotune_nb(1024, precision)
     try:
-        assert best in (16, 32, 64)
-        assert all(m > 0 for m in ms)
+        assert best in (16, 32, 64, 128)
+        assert len(ms) == 4 and all(m > 0 for m in ms)
         assert gpu.zq_tuned_nb(1024, 0 if precision == "fp64" else 1) == best
         # solves in the tuned bucket still meet the accuracy bar
         n = 600
@@ -48,19 +48,25 @@ def test_batch_plan_matches_batched_call(gpu):
 
     ns, offs, eoffs, master = _batch(300, 900)
     n2s = (2 * ns).astype(np.int32)
-    ref = master.clone()
-    eref = torch.zeros(int(ns.sum()), dtype=torch.float64, device="cuda")
     st = torch.cuda.current_stream().cuda_stream
-    assert gpu.zquatev_batched_device(len(ns), n2s.ctypes.data, n2s.ctypes.data, offs.ctypes.data, eoffs.ctypes.data,
-                                      ref.data_ptr(), eref.data_ptr(), st) == 0
     plan = solver.BatchPlan(n2s, n2s, offs, eoffs)
     work = master.clone()
-    e = torch.zeros_like(eref)
-    plan.run(work, e)  # tunes the launch shape, captures, replays
+    e = torch.zeros(int(ns.sum()), dtype=torch.float64, device="cuda")
+    plan.run(work, e)  # tunes the launch shape and the per-size variant, captures, replays
     assert plan.info() == 0
     shape = plan.shape()
     assert 1 <= shape["ctas_per_sm"] <= 4 and shape["ctas"] >= 1
-    # one CTA solves one matrix whatever the launch shape: results are identical
+    assert shape["warp_max_n"] in (0, 16, 24, 32) and all(v > 0 for v in shape["variant_ms"].values())
+    # the unplanned call with the same variant switch: each matrix is solved by
+    # the same kind of group whatever the launch shape, so results are identical
+    assert gpu.zq_set_batch_warp_max(shape["warp_max_n"]) == 0
+    try:
+        ref = master.clone()
+        eref = torch.zeros_like(e)
+        assert gpu.zquatev_batched_device(len(ns), n2s.ctypes.data, n2s.ctypes.data, offs.ctypes.data,
+                                          eoffs.ctypes.data, ref.data_ptr(), eref.data_ptr(), st) == 0
+    finally:
+        gpu.zq_set_batch_warp_max(-1)
     assert torch.equal(work, ref) and torch.equal(e, eref)
     for _ in range(2):  # replays of the captured graph
         work.copy_(master)
@@ -100,3 +106,39 @@ def test_batch_plan_fixed_shape_and_pointer_change(gpu):
 def test_batch_plan_rejects_large(gpu):
     with pytest.raises(_lib.ZquatevError):
         solver.BatchPlan([514], [514], [0], [0])
+
+
+def test_batch_variants_agree(gpu):
+    """The warp-per-matrix variant (orders <= 32) and the CTA-per-matrix one
+    give the same eigenpairs within the parity tolerance."""
+    import torch
+
+    ns, offs, eoffs, master = _batch(120, 4400)
+    assert (ns <= 32).sum() >= 20  # log-uniform in [2, 256]: plenty for the warp variant
+    n2s = (2 * ns).astype(np.int32)
+    st = torch.cuda.current_stream().cuda_stream
+    outs = []
+    for wmax in (0, 32):
+        assert gpu.zq_set_batch_warp_max(wmax) == 0
+        try:
+            work = master.clone()
+            e = torch.zeros(int(ns.sum()), dtype=torch.float64, device="cuda")
+            assert gpu.zquatev_batched_device(len(ns), n2s.ctypes.data, n2s.ctypes.data, offs.ctypes.data,
+                                              eoffs.ctypes.data, work.data_ptr(), e.data_ptr(), st) == 0
+        finally:
+            gpu.zq_set_batch_warp_max(-1)
+        outs.append((work.cpu().numpy(), e.cpu().numpy()))
+    (w0, e0), (w1, e1) = outs
+    for i in range(len(ns)):
+        n = int(ns[i])
+        d = master[offs[i]:offs[i] + 4 * n * n].cpu().numpy().reshape(2 * n, 2 * n, order="F")
+        h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
+        o1 = w1[offs[i]:offs[i] + 4 * n * n].reshape(2 * n, 2 * n, order="F")
+        o0 = w0[offs[i]:offs[i] + 4 * n * n].reshape(2 * n, 2 * n, order="F")
+        l0, l1 = e0[eoffs[i]:eoffs[i] + n], e1[eoffs[i]:eoffs[i] + n]
+        hn = metrics.h_norm2(l0)
+        assert metrics.eig_error(l1, l0, hn) <= 1e-12
+        assert metrics.residual(h, o1, l1) <= 1e-12
+        assert metrics.orthonormality(o1) <= 1e-12
+        assert metrics.structure_exact(o1, n)
+        assert metrics.subspace_distance(o1, l1, o0, l0, 1e-6 * hn) < 1e-8

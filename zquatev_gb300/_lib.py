@@ -53,6 +53,8 @@ SIGNATURES = {
     "zq_batch_plan_info": (_c_int, [_vp, _vp]),
     "zq_batch_plan_shape": (_c_int, [_vp, _vp, _vp, _vp]),
     "zq_batch_plan_destroy": (_c_int, [_vp]),
+    "zq_batch_plan_variant": (_c_int, [_vp, _vp, _vp]),
+    "zq_set_batch_warp_max": (_c_int, [_c_int]),
     "zq_server_create": (_vp, [_c_ll, _c_int, _c_int, _c_int]),
     "zq_server_submit": (_c_ll, [_vp, _c_int, _vp, _c_int, _vp]),
     "zq_server_test": (_c_int, [_vp, _c_ll]),

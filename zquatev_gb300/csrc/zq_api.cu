@@ -118,7 +118,7 @@ void nb_table_set(int prec, int n, int nb) { g_nb_table[prec & 1][nb_bucket(n)].
 int nb_table_get(int prec, int n) { return g_nb_table[prec & 1][nb_bucket(n)].load(); }
 
 static int nb_for(int n, int prec = 0) {
-  if (const char* s = getenv("ZQ_NB")) { const int v = atoi(s); if (v >= 1 && v <= 64) return v; }
+  if (const char* s = getenv("ZQ_NB")) { const int v = atoi(s); if (v >= 1 && v <= NBMAX) return v; }
   if (const int t = nb_table_get(prec, n)) return t;
   return g_nb;
 }
@@ -205,7 +205,7 @@ static Layout layout_for(int n, int nbmax, int nbq, size_t nnodes, size_t ndescs
 void solve_workspace_bytes(int n, size_t* fp64_bytes, size_t* refine_bytes) {
   DcPlan probe;
   probe.build(n);
-  const Layout L = layout_for(n, 64, g_nbq, probe.num_nodes(), probe.num_descs());
+  const Layout L = layout_for(n, NBMAX, g_nbq, probe.num_nodes(), probe.num_descs());
   if (fp64_bytes) *fp64_bytes = L.total;
   if (refine_bytes) *refine_bytes = refine_workspace_bytes(n, g_nbq) + ozaki_workspace_bytes(n) + 4096 + 256;
 }
@@ -255,7 +255,7 @@ int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool
   if (c->dc_n != n) {
     DcPlan probe;
     probe.build(n);
-    Layout L = layout_for(n, 64, nbq, probe.num_nodes(), probe.num_descs());
+    Layout L = layout_for(n, NBMAX, nbq, probe.num_nodes(), probe.num_descs());
     if (int rc = ensure_ws(c, L.total)) return rc;
     c->dc = probe;
     char* base = reinterpret_cast<char*>(c->ws);
@@ -266,7 +266,7 @@ int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool
     if (int rc = c->dc.upload(dcws, nodes, descs, c->st)) return rc;
     c->dc_n = n;
   }
-  Layout L = layout_for(n, 64, nbq, c->dc.num_nodes(), c->dc.num_descs());
+  Layout L = layout_for(n, NBMAX, nbq, c->dc.num_nodes(), c->dc.num_descs());
   char* base = reinterpret_cast<char*>(c->ws);
   void* tri_ws = base;
   double* sm = reinterpret_cast<double*>(base + L.tri);
@@ -284,7 +284,7 @@ int solve_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, bool
   ZQ_CUDA(cudaStreamWaitEvent(c->st, c->ev_fork, 0));
 
   tm.mark("start", c->st);
-  TridiagView<double> v = tridiag_bind<double>(tri_ws, dD, n, ldd, 64, d, e, tau);
+  TridiagView<double> v = tridiag_bind<double>(tri_ws, dD, n, ldd, NBMAX, d, e, tau);
   prof_begin(PC_TRIDIAG, c->st);
   if (int rc = tridiagonalize<double>(v, nb, c->st)) return rc;
   prof_end(PC_TRIDIAG, c->st);
@@ -426,7 +426,7 @@ int ensure_plan(Context* c, int n) {
   if (c->dc_n == n) return ZQ_OK;
   DcPlan probe;
   probe.build(n);
-  Layout L = layout_for(n, 64, g_nbq, probe.num_nodes(), probe.num_descs());
+  Layout L = layout_for(n, NBMAX, g_nbq, probe.num_nodes(), probe.num_descs());
   if (int rc = ensure_ws(c, L.total)) return rc;
   c->dc = probe;
   char* base = reinterpret_cast<char*>(c->ws);
@@ -448,7 +448,7 @@ int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cu
     ZQ_CUDA(cudaMalloc(&rb.dev, need));
     rb.bytes = need;
   }
-  Layout L = layout_for(n, 64, g_nbq, c->dc.num_nodes(), c->dc.num_descs());
+  Layout L = layout_for(n, NBMAX, g_nbq, c->dc.num_nodes(), c->dc.num_descs());
   DgemmDesc* desc1 = reinterpret_cast<DgemmDesc*>(reinterpret_cast<char*>(c->ws) + L.tri + L.small + L.dc + L.fq + L.nodes) +
                      c->dc.num_descs();
   RefineArgs ra{};
@@ -638,7 +638,7 @@ int zq_stedc_device(int n, const double* d, const double* e, double* lam, double
   if (c->dc_n != n) {
     DcPlan probe;
     probe.build(n);
-    Layout L = layout_for(n, 64, g_nbq, probe.num_nodes(), probe.num_descs());
+    Layout L = layout_for(n, NBMAX, g_nbq, probe.num_nodes(), probe.num_descs());
     if (int rc = ensure_ws(c, L.total)) return rc;
     c->dc = probe;
     char* base = reinterpret_cast<char*>(c->ws);
@@ -726,7 +726,7 @@ int zq_profile_flops(int cls, double* flops) {
 }
 
 int zq_set_block_size(int nb) {
-  if (nb < 1 || nb > 64) { set_msg("block size must be in [1, 64]"); return ZQ_ERR_ARG; }
+  if (nb < 1 || nb > NBMAX) { set_msg("block size must be in [1, 128]"); return ZQ_ERR_ARG; }
   g_nb = nb;
   for (auto& row : g_nb_table)
     for (auto& v : row) v.store(0);  // an explicit width replaces the tuned table

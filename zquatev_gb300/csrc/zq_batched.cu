@@ -22,6 +22,8 @@
 #include "zq_common.cuh"
 #include "zq_kernels.h"
 
+#include <atomic>
+#include <cstdlib>
 #include <mutex>
 
 namespace zq {
@@ -50,25 +52,52 @@ struct BatchArgs {
   int* info;        // per task: 0 ok, >0 QL non-convergence
 };
 
-__device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double* ws) {
+// Shared memory of one solving group: a CTA (G = 256, n <= 256) or a warp
+// (G = 32, n <= 32).
+template <int NM>
+struct GroupSmem {
+  double2 swa[NM], swb[NM], sya[NM], syb[NM];
+  double sc[NM], ss[NM];
+  double sred[8];
+  double sscal[8];
+  int sflag[2];
+  int s_m, s_cnt, s_done;
+};
+template <int G> __device__ __forceinline__ void gsync() {
+  if (G == 32) __syncwarp(); else __syncthreads();
+}
+template <int G> __device__ __forceinline__ double gsum(double v, double* sh) {
+  if (G == 32) return warp_sum(v);
+  return block_sum(v, sh);
+}
+template <int G> __device__ __forceinline__ double gmax(double v, double* sh) {
+  if (G == 32) return warp_max(v);
+  return block_max(v, sh);
+}
+
+template <int G, int NM>
+__device__ void batch_solve_group(const BatchTask& tk, const BatchArgs& a, double* ws, GroupSmem<NM>& sm, int tid) {
   const int n = tk.n;
   const int64_t ld = tk.ld;
   double2* A = tk.Dp ? tk.Dp : a.D + tk.off;
   double2* B = A + n;
-  const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
-  __shared__ double2 swa[BNMAX], swb[BNMAX], sya[BNMAX], syb[BNMAX];
-  __shared__ double sred[BT / 32];
-  __shared__ double sscal[8];
-  __shared__ double sc_[BNMAX], ss_[BNMAX];   // QL rotations of one sweep
-  __shared__ int sflag[2];
+  double2* swa = sm.swa;
+  double2* swb = sm.swb;
+  double2* sya = sm.sya;
+  double2* syb = sm.syb;
+  double* sred = sm.sred;
+  double* sscal = sm.sscal;
+  double* sc_ = sm.sc;     // QL rotations of one sweep
+  double* ss_ = sm.ss;
+  int* sflag = sm.sflag;
   double* d = ws;                 // n
-  double* e4 = d + BNMAX;         // 4n quaternion subdiagonal
-  double* offd = e4 + 4 * BNMAX;  // n
-  double* phi = offd + BNMAX;     // 4n
-  double* rank_d = phi + 4 * BNMAX;  // n (eigenvalues, QL output)
-  int* perm = reinterpret_cast<int*>(rank_d + BNMAX);  // n
-  double* Z = rank_d + 2 * BNMAX;  // n x n, column-major, ld n
+  double* e4 = d + NM;            // 4n quaternion subdiagonal
+  double* offd = e4 + 4 * NM;     // n
+  double* phi = offd + NM;        // 4n
+  double* rank_d = phi + 4 * NM;  // n (eigenvalues, QL output)
+  int* perm = reinterpret_cast<int*>(rank_d + NM);  // n
+  double* Z = rank_d + 2 * NM;    // n x n, column-major, ld n
 
   // ---------------------------------------------------------------- step 1
   for (int j = 0; j < n; ++j) {
@@ -77,21 +106,21 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
     if (L < 1) break;
     // norm of x = (A[j+1:, j], B[j+1:, j]) (max-scaled)
     double mx = 0.0;
-    for (int i = tid; i < L; i += BT) {
+    for (int i = tid; i < L; i += G) {
       const double2 xa = A[j + 1 + i + (int64_t)j * ld], xb = B[j + 1 + i + (int64_t)j * ld];
       mx = fmax(mx, fmax(fmax(fabs(xa.x), fabs(xa.y)), fmax(fabs(xb.x), fabs(xb.y))));
     }
-    mx = block_max(mx, sred);
+    mx = gmax<G>(mx, sred);
     double ssq = 0.0;
     if (mx > 0.0) {
       const double inv = 1.0 / mx;
-      for (int i = tid; i < L; i += BT) {
+      for (int i = tid; i < L; i += G) {
         const double2 xa = A[j + 1 + i + (int64_t)j * ld], xb = B[j + 1 + i + (int64_t)j * ld];
         const double a0 = xa.x * inv, a1 = xa.y * inv, b0 = xb.x * inv, b1 = xb.y * inv;
         ssq += a0 * a0 + a1 * a1 + b0 * b0 + b1 * b1;
       }
     }
-    ssq = block_sum(ssq, sred);
+    ssq = gsum<G>(ssq, sred);
     if (tid == 0) {
       const double nu = mx * sqrt(ssq);
       const double2 qa = A[j + 1 + (int64_t)j * ld], qb = B[j + 1 + (int64_t)j * ld];
@@ -116,10 +145,10 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
       e4[4 * j] = ee0; e4[4 * j + 1] = ee1; e4[4 * j + 2] = ee2; e4[4 * j + 3] = ee3;
       sscal[0] = f; sscal[1] = m0 * f; sscal[2] = m1 * f; sscal[3] = m2 * f; sscal[4] = m3 * f;
     }
-    __syncthreads();
+    gsync<G>();
     const double f = sscal[0];
     // w in place of x (and in shared memory)
-    for (int i = tid; i < L; i += BT) {
+    for (int i = tid; i < L; i += G) {
       double2 wa = make_double2(0, 0), wb = wa;
       if (f > 0.0) {
         if (i == 0) { wa = make_double2(sscal[1], sscal[2]); wb = make_double2(sscal[3], sscal[4]); }
@@ -129,12 +158,12 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
       B[j + 1 + i + (int64_t)j * ld] = wb;
       swa[i] = wa; swb[i] = wb;
     }
-    __syncthreads();
+    gsync<G>();
     if (f == 0.0) continue;
     // g = H_trail w  (rows j+1.., thread per row; lower triangles only)
     const int r0 = j + 1;
     double cp = 0.0;
-    for (int i = tid; i < L; i += BT) {
+    for (int i = tid; i < L; i += G) {
       double2 ax = make_double2(0, 0), az = ax, bx = ax, bz = ax;
       const int gi = r0 + i;
       // the three ranges of c (row i left of the diagonal, the diagonal, column
@@ -164,15 +193,15 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
       sya[i] = ga; syb[i] = gb;
       cp += swa[i].x * ga.x + swa[i].y * ga.y + swb[i].x * gb.x + swb[i].y * gb.y;
     }
-    const double c = block_sum(cp, sred);
-    for (int i = tid; i < L; i += BT) {
+    const double c = gsum<G>(cp, sred);
+    for (int i = tid; i < L; i += G) {
       sya[i] = csub(sya[i], cscale(swa[i], 0.5 * c));
       syb[i] = csub(syb[i], cscale(swb[i], 0.5 * c));
     }
-    __syncthreads();
+    gsync<G>();
     // rank-2 structured update of the trailing lower triangles: each thread
     // walks its row's segment (independent elements, so the loads pipeline)
-    for (int i = tid; i < L; i += BT) {
+    for (int i = tid; i < L; i += G) {
       const double2 wai = swa[i], wbi = swb[i], yai = sya[i], ybi = syb[i];
       const int64_t orow = r0 + i;
 #pragma unroll 4
@@ -194,9 +223,9 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
         A[o] = csub(A[o], ta);
       }
     }
-    __syncthreads();
+    gsync<G>();
   }
-  __syncthreads();
+  gsync<G>();
 
   // ---------------------------------------------------------------- step 2
   if (tid == 0) {
@@ -222,15 +251,17 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
     sflag[0] = 0;
   }
   // Z = I
-  for (int t = tid; t < n * n; t += BT) Z[t] = ((t % n) == (t / n)) ? 1.0 : 0.0;
-  __syncthreads();
+  for (int t = tid; t < n * n; t += G) Z[t] = ((t % n) == (t / n)) ? 1.0 : 0.0;
+  gsync<G>();
 
   // ---------------------------------------------------------------- step 3
   // implicit QL with Wilkinson shift; d <- eigenvalues, Z <- eigenvectors
   const double eps = 1.1102230246251565e-16;
   for (int l = 0; l < n; ++l) {
     for (int iter = 0;; ++iter) {
-      __shared__ int s_m, s_cnt, s_done;
+      int& s_m = sm.s_m;
+      int& s_cnt = sm.s_cnt;
+      int& s_done = sm.s_done;
       if (tid == 0) {
         int m = l;
         for (; m < n - 1; ++m) {
@@ -264,13 +295,13 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
           s_m = m;
         }
       }
-      __syncthreads();
+      gsync<G>();
       if (s_done) break;
       // apply the sweep's rotations (columns m-1 .. lo of Z) to every row
       const int m = s_m, cnt = s_cnt;
       // the updated column i of one rotation is column i + 1 of the next: carry
       // it in a register (no reload of a value just stored)
-      for (int r = tid; r < n; r += BT) {
+      for (int r = tid; r < n; r += G) {
         double* zr = Z + r;
         if (cnt == 0) continue;
         double carry = zr[(int64_t)m * n];
@@ -283,37 +314,37 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
         }
         zr[(int64_t)(m - cnt) * n] = carry;
       }
-      __syncthreads();
+      gsync<G>();
     }
   }
   // ascending order: rank of each eigenvalue (ties by index)
-  for (int k = tid; k < n; k += BT) {
+  for (int k = tid; k < n; k += G) {
     const double v = d[k];
     int rnk = 0;
     for (int q = 0; q < n; ++q) rnk += (d[q] < v) || (d[q] == v && q < k);
     perm[rnk] = k;
   }
-  __syncthreads();
+  gsync<G>();
 
   // ---------------------------------------------------------------- step 4
   // X = Phi Z (sorted columns) in the right half: X_a[r, col] = alpha_r z_r, X_b = beta_r z_r
   double2* XA = A + (int64_t)n * ld;
   double2* XB = XA + n;
-  for (int t = tid; t < n * n; t += BT) {
+  for (int t = tid; t < n * n; t += G) {
     const int r = t % n, col = t / n;
     const double z = Z[r + (int64_t)perm[col] * n];
     XA[r + (int64_t)col * ld] = make_double2(phi[4 * r] * z, phi[4 * r + 1] * z);
     XB[r + (int64_t)col * ld] = make_double2(phi[4 * r + 2] * z, phi[4 * r + 3] * z);
   }
   double* eig_out = tk.Ep ? tk.Ep : a.eig + tk.eoff;
-  for (int k = tid; k < n; k += BT) eig_out[k] = d[perm[k]];
-  __syncthreads();
+  for (int k = tid; k < n; k += G) eig_out[k] = d[perm[k]];
+  gsync<G>();
   // reflectors backwards: x <- x - w <w,x> - w' [w,x], w' = (-conj(wb), conj(wa))
   for (int j = n - 3; j >= 0; --j) {
     const int L = n - 1 - j;
-    for (int i = tid; i < L; i += BT) { swa[i] = A[j + 1 + i + (int64_t)j * ld]; swb[i] = B[j + 1 + i + (int64_t)j * ld]; }
-    __syncthreads();
-    for (int col = warp; col < n; col += BT / 32) {
+    for (int i = tid; i < L; i += G) { swa[i] = A[j + 1 + i + (int64_t)j * ld]; swb[i] = B[j + 1 + i + (int64_t)j * ld]; }
+    gsync<G>();
+    for (int col = warp; col < n; col += G / 32) {
       double2* xa = XA + (j + 1) + (int64_t)col * ld;
       double2* xb = XB + (j + 1) + (int64_t)col * ld;
       double2 c1 = make_double2(0, 0), c2 = c1;
@@ -335,10 +366,10 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
         xb[i] = csub(vb, tb);
       }
     }
-    __syncthreads();
+    gsync<G>();
   }
   // output: left half (U; V) = X, right half (-conj(V); conj(U))
-  for (int t = tid; t < n * n; t += BT) {
+  for (int t = tid; t < n * n; t += G) {
     const int r = t % n, col = t / n;
     const double2 u = XA[r + (int64_t)col * ld], vv = XB[r + (int64_t)col * ld];
     A[r + (int64_t)col * ld] = u;
@@ -347,20 +378,61 @@ __device__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double*
     XB[r + (int64_t)col * ld] = make_double2(u.x, -u.y);
   }
   if (tid == 0) a.info[tk.out_slot] = sflag[0];
-  __syncthreads();
+  gsync<G>();
 }
 
-__global__ void __launch_bounds__(BT, 3) k_batched(BatchArgs a) {
+// Per-size variants in one persistent launch. Tasks come largest first; a CTA
+// takes one at a time and solves it with all 256 threads while n > wmax. The
+// first task of at most wmax (the autotuned switch size, <= 32) turns the CTA
+// into eight independent warps: each warp solves whole matrices (one lane per
+// row, warp-synchronous steps) and takes further tasks from the same counter,
+// all of which are small from then on.
+constexpr int WNM = 32;  // largest order a warp solves
+constexpr long long WARP_WS = 12LL * WNM + (long long)WNM * WNM + 64;  // per-warp workspace (doubles)
+union BatchSmem {
+  GroupSmem<BNMAX> cta;
+  GroupSmem<WNM> warp[BT / 32];
+};
+__device__ __forceinline__ void batch_solve_one(const BatchTask& tk, const BatchArgs& a, double* ws) {
+  __shared__ BatchSmem s_one;
+  batch_solve_group<BT, BNMAX>(tk, a, ws, s_one.cta, threadIdx.x);
+}
+
+__global__ void __launch_bounds__(BT, 3) k_batched(BatchArgs a, int wmax) {
   __shared__ int s_task;
+  __shared__ BatchSmem smem;
   double* ws = a.ws + (int64_t)blockIdx.x * a.ws_stride;
+  int t;
   for (;;) {
     if (threadIdx.x == 0) s_task = atomicAdd(a.counter, 1);
     __syncthreads();
-    const int t = s_task;
+    t = s_task;
     __syncthreads();
-    if (t >= a.count) break;
+    if (t >= a.count) return;
+    if (a.tasks[t].n <= wmax) break;  // the rest of the queue is small: warp mode
     const BatchTask tk = a.tasks[t];
-    if (tk.n > 0) batch_solve_one(tk, a, ws);
+    if (tk.n > 0) batch_solve_group<BT, BNMAX>(tk, a, ws, smem.cta, threadIdx.x);
+  }
+  // warp mode: warp 0 starts with task t, the others take their own
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* wws = ws + (int64_t)warp * WARP_WS;
+  GroupSmem<WNM>& wsm = smem.warp[warp];
+  if (warp != 0) {
+    int nt = 0;
+    if (lane == 0) nt = atomicAdd(a.counter, 1);
+    t = __shfl_sync(0xffffffffu, nt, 0);
+  }
+  while (t < a.count) {
+    const BatchTask tk = a.tasks[t];
+    if (tk.n > WNM) {
+      // a queue not sorted largest first: never solve above the warp's size
+      if (lane == 0) a.info[tk.out_slot] = -1;
+    } else if (tk.n > 0) {
+      batch_solve_group<32, WNM>(tk, a, wws, wsm, lane);
+    }
+    int nt = 0;
+    if (lane == 0) nt = atomicAdd(a.counter, 1);
+    t = __shfl_sync(0xffffffffu, nt, 0);
   }
 }
 
@@ -370,8 +442,23 @@ long long batched_ws_stride() {
 }
 int batched_max_n() { return BNMAX; }
 
+// switch size of the warp variant for launches that are not autotuned
+// (environment ZQ_BATCH_WARP_MAX overrides; 0 disables the warp variant)
+static std::atomic<int> g_warp_max{-1};
+int batched_warp_max() {
+  int v = g_warp_max.load();
+  if (v < 0) {
+    v = 24;
+    if (const char* e = getenv("ZQ_BATCH_WARP_MAX")) v = atoi(e);
+    v = v < 0 ? 0 : (v > WNM ? WNM : v);
+    g_warp_max.store(v);
+  }
+  return v;
+}
+void batched_set_warp_max(int v) { g_warp_max.store(v < 0 ? -1 : (v > WNM ? WNM : v)); }
+
 int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
-                   int ctas, int* dev_info, cudaStream_t st) {
+                   int ctas, int* dev_info, cudaStream_t st, int wmax) {
   if (count <= 0) return ZQ_OK;
   BatchArgs a{};
   a.tasks = reinterpret_cast<const BatchTask*>(dev_tasks);
@@ -384,7 +471,8 @@ int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* 
   a.info = dev_info;
   ZQ_CUDA(cudaMemsetAsync(dev_counter, 0, sizeof(int), st));
   prof_begin(PC_BATCHED, st);
-  k_batched<<<ctas, BT, 0, st>>>(a);
+  if (wmax < 0) wmax = batched_warp_max();
+  k_batched<<<ctas, BT, 0, st>>>(a, wmax > WNM ? WNM : wmax);
   prof_end(PC_BATCHED, st);
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;

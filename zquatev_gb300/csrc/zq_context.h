@@ -67,8 +67,12 @@ int nb_table_get(int prec, int n);
 // batched kernel (zq_batched.cu)
 long long batched_ws_stride();
 int batched_max_n();
+// wmax: largest order solved by the warp variant (tasks sorted largest first;
+// -1: the current default, 0: CTA variant only)
 int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
-                   int ctas, int* dev_info, cudaStream_t st);
+                   int ctas, int* dev_info, cudaStream_t st, int wmax = -1);
+int batched_warp_max();
+void batched_set_warp_max(int v);
 size_t batched_task_bytes();
 void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot);
 // task addressing its matrix and eigenvalues by pointer (D, eig of the launch unused for it)

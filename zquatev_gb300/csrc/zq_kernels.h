@@ -10,6 +10,9 @@
 namespace zq {
 
 // ---------------------------------------------------------------- tridiagonal
+// widest panel of the blocked reduction (reflectors kept per panel)
+constexpr int NBMAX = 128;
+
 template <typename R>
 struct TridiagView {
   cplx<R>* M;      // [A; B], 2n x n, column-major

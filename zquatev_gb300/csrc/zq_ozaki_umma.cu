@@ -98,10 +98,34 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatil
 }
 // Bounded wait that ignores the abort flag (clean-up of work in flight): always
 // the default limit, as copies and MMAs already issued finish in microseconds.
-__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity) {
+__device__ __forceinline__ void mbar_drain(uint32_t bar, uint32_t parity, long long limit = UM_WAIT_CYCLES) {
   const long long t0 = clock64();
-  while (!mbar_try(bar, parity) && clock64() - t0 <= UM_WAIT_CYCLES) {
+  while (!mbar_try(bar, parity) && clock64() - t0 <= limit) {
   }
+}
+
+// the same box written to this CTA and its cluster peer (same shared offsets);
+// complete_tx is signalled on the mbarrier at `bar` in each destination
+__device__ __forceinline__ void tma_2d_mc(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%2, %3}], "
+      "[%4], %5;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                   bar),
+               "h"(mask)
+               : "memory");
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
 }
 
 __device__ __forceinline__ void tma_2d(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar) {
@@ -142,6 +166,14 @@ __device__ __forceinline__ double um_pow2i(int E) {
   return __longlong_as_double((long long)(1023 + E) << 52);
 }
 
+// MC: launched as clusters of two CTAs on vertically adjacent tiles of the
+// same column tile, which share the B operand: each CTA loads its own A box and
+// one half of B (rank 0 the real part, rank 1 the imaginary part) multicast to
+// both, so a CTA reads 32 KB per stage from L2 instead of 48 KB. A stage is
+// refilled once both CTAs' MMAs have released it (the MMA commit arrives on
+// both CTAs' empty barriers). A cluster's second tile past the last row tile is
+// computed but not written.
+template <bool MC>
 __global__ void __launch_bounds__(UM_THREADS, 1)
     k_oz_umma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBr,
               const __grid_constant__ CUtensorMap tmBi, UmArgs g) {
@@ -160,7 +192,7 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   if (threadIdx.x == 0) {
     for (int s = 0; s < UM_STAGES; ++s) {
       mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, MC ? 2 : 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(accf0 + 8 * b, 1);
@@ -180,11 +212,30 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  if (MC) cluster_sync();  // the peer's barriers are initialised before any multicast or remote arrival
   const uint32_t tmem = s_tmem;
   volatile int* abort = &s_abort;
+  const uint32_t rank = MC ? cluster_rank() : 0u;
 
   int bi, bj;
-  if (g.lower) {
+  if (MC) {
+    const int tm = g.mp / UM_BM, tn = g.np / UM_BN;
+    const int p = (int)(blockIdx.x >> 1);
+    if (g.lower) {
+      // pairs (bj + 2q, bj + 2q + 1) down column bj, columns in order
+      int col = 0, first = 0;
+      while (col + 1 < tm && p >= first + (tm - col + 1) / 2) { first += (tm - col + 1) / 2; ++col; }
+      bj = col;
+      bi = col + 2 * (p - first) + (int)rank;
+    } else {
+      // groups of UM_GROUP / 2 row-tile pairs sweep the column tiles together
+      const int P = (tm + 1) / 2, G2 = UM_GROUP / 2;
+      const int per = G2 * tn, grp = p / per, firstp = grp * G2;
+      const int gm = (P - firstp) < G2 ? (P - firstp) : G2;
+      bi = 2 * (firstp + (p % per) % gm) + (int)rank;
+      bj = (p % per) / gm;
+    }
+  } else if (g.lower) {
     tri_tile((int)blockIdx.x, bi, bj);
   } else {
     // grouped order: runs of UM_GROUP row tiles sweep the column tiles
@@ -214,15 +265,22 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
           const int t = (int)(kg / Kp), kk = (int)(kg % Kp), u = lev - t;
           mbar_expect_tx(full0 + 8 * stage, UM_STAGE_BYTES);
           tma_2d(sA, &tmA, kk, t * g.mp + i0, full0 + 8 * stage);
-          tma_2d(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage);
-          tma_2d(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage);
+          if (MC) {
+            if (rank == 0) tma_2d_mc(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage, (uint16_t)3);
+            else tma_2d_mc(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage, (uint16_t)3);
+          } else {
+            tma_2d(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage);
+            tma_2d(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage);
+          }
           ++ks;
         }
       }
       issued = ks;
-      // copies in flight finish before the CTA may exit
+      // copies in flight finish before the CTA may exit (after an abort in a
+      // cluster a stage may lack the peer's half and never complete: its own
+      // copies land within microseconds, so wait about a millisecond there)
       for (int q = (issued > UM_STAGES ? issued - UM_STAGES : 0); q < issued; ++q)
-        mbar_drain(full0 + 8 * (q % UM_STAGES), (q / UM_STAGES) & 1);
+        mbar_drain(full0 + 8 * (q % UM_STAGES), (q / UM_STAGES) & 1, MC ? 2000000LL : UM_WAIT_CYCLES);
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
@@ -248,7 +306,8 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
 #pragma unroll
               for (int k = 0; k < UM_BK / 16; ++k)  // 16 bf16 = 32 bytes along the swizzled row
                 umma_bf16(d, ad + 2 * k, bd + 2 * k, (kg != cb || k > 0) ? 1u : 0u);
-              umma_commit(empty0 + 8 * stage);
+              if (MC) umma_commit_mc(empty0 + 8 * stage, (uint16_t)3);
+              else umma_commit(empty0 + 8 * stage);
               ++ks;
             }
             if (!ok) break;
@@ -332,6 +391,8 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   tc_fence_after();
   if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
   if (threadIdx.x == 0 && s_abort) atomicExch(g.err, 1);
+  // neither CTA leaves while its peer may still multicast into it or arrive on its barriers
+  if (MC) cluster_sync();
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -379,7 +440,7 @@ long long pipeline_wait_cycles() { return g_wait_cycles.load(); }
 // err: device int, zeroed here, raised by the kernel on a wait timeout.
 int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_bfloat16* Bis, int mp, int np, int Kp,
                  int m, int n, int nsl, int lower, const int* ea, const int* eb, double2* C, int64_t ldc, int* err,
-                 cudaStream_t st) {
+                 cudaStream_t st, bool multicast) {
   if (mp % UM_BM || np % UM_BN || Kp % UM_BK || nsl < 1) { set_error_message("oz_umma_gemm: bad padding"); return ZQ_ERR_ARG; }
   CUtensorMap ta, tbr, tbi;
   if (int rc = make_map(&ta, As, Kp, (int64_t)nsl * mp)) return rc;
@@ -391,7 +452,8 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
     ZQ_CUDA(cudaGetDevice(&dev));
     const unsigned long long bit = 1ull << (dev & 63);
     if (!(attr_set.load() & bit)) {
-      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
       attr_set.fetch_or(bit);
     }
   }
@@ -400,9 +462,29 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
   a.ea = ea; a.eb = eb; a.C = C; a.ldc = ldc; a.err = err;
   a.wait = g_wait_cycles.load();
   const int tm = mp / UM_BM, tn = np / UM_BN;
-  const dim3 grid = lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)(tm * tn), 1);
   ZQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-  k_oz_umma<<<grid, UM_THREADS, UM_SMEM, st>>>(ta, tbr, tbi, a);
+  if (multicast) {
+    // clusters of two row-adjacent tiles (the last pair of a column may hold a tile past the matrix)
+    int pairs = 0;
+    if (lower) for (int col = 0; col < tm; ++col) pairs += (tm - col + 1) / 2;
+    else pairs = ((tm + 1) / 2) * tn;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(2 * pairs), 1, 1);
+    cfg.blockDim = dim3(UM_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = UM_SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ZQ_CUDA(cudaLaunchKernelEx(&cfg, k_oz_umma<true>, ta, tbr, tbi, a));
+  } else {
+    const dim3 grid = lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)(tm * tn), 1);
+    k_oz_umma<false><<<grid, UM_THREADS, UM_SMEM, st>>>(ta, tbr, tbi, a);
+  }
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;
 }

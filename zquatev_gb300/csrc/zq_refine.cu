@@ -427,7 +427,7 @@ size_t refine_workspace_bytes(int n, int nbq) {
   b += sizeof(double2) * 2 * nn;        // HX
   b += sizeof(double2) * 4 * nn;        // G1, G2, S1, S2
   b += sizeof(double2) * 2 * nn;        // Et, Eb
-  b += tridiag_workspace_bytes<float>(n, 64);
+  b += tridiag_workspace_bytes<float>(n, NBMAX);
   b += form_q_workspace_bytes(n, nbq);  // sized for double2, enough for float2
   b += sizeof(double) * (46 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64);
   b += sizeof(int) * (size_t)n;
@@ -462,7 +462,7 @@ static int zgemm_acc(int mode, int opa1, int opb1, int opa2, int opb2, const Zge
 long long batched_ws_stride();
 int batched_max_n();
 int batched_launch(const void* dev_tasks, int count, int* dev_counter, double2* D, double* eig, double* ws,
-                   int ctas, int* dev_info, cudaStream_t st);
+                   int ctas, int* dev_info, cudaStream_t st, int wmax);
 size_t batched_task_bytes();
 void batched_fill_task(void* dst, long long off, long long eoff, int n, int ld, int slot);
 
@@ -544,7 +544,8 @@ static int resolve_clusters(RefineArgs& ra, double2* X, int64_t ldd, double2* S1
   ZQ_CUDA(cudaMemcpyAsync(dtasks, htasks.data(), tb * ncl, cudaMemcpyHostToDevice, st));
   k_cl_gather<<<ncl, 256, 0, st>>>(S1, S2, G1, G2, n, lam, dmem, dcs, dco, ncl, blocks);
   ZQ_LAUNCH_CHECK();
-  if (int rc = batched_launch(dtasks, ncl, dinf + ncl, blocks, ceig, bws, ctas, dinf, st)) return rc;
+  // cluster blocks are not queued by size: one CTA per block (no warp variant)
+  if (int rc = batched_launch(dtasks, ncl, dinf + ncl, blocks, ceig, bws, ctas, dinf, st, 0)) return rc;
   // X_C (2n x m scratch in tmpa)
   const int gx = ceil_div(2 * n * kmax, 256) > 64 ? 64 : ceil_div(2 * n * kmax, 256);
   k_cl_rotate<<<dim3(gx, ncl), 256, 0, st>>>(X, ldd, n, dmem, dcs, dco, deo, ncl, blocks, ceig, tmpa, lam);
@@ -585,7 +586,7 @@ int refined_solve(RefineArgs& ra) {
   double2* S2 = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
   double2* Et = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
   double2* Eb = reinterpret_cast<double2*>(take(sizeof(double2) * nn));
-  void* tri_ws = take(tridiag_workspace_bytes<float>(n, 64));
+  void* tri_ws = take(tridiag_workspace_bytes<float>(n, NBMAX));
   void* fq_ws = take(form_q_workspace_bytes(n, ra.nbq));
   double* sm = reinterpret_cast<double*>(take(sizeof(double) * (46 * (size_t)n + 3 * 8192 + 8192 + 2048 + 64)));
   int* rank = reinterpret_cast<int*>(take(sizeof(int) * (size_t)n));
@@ -620,7 +621,7 @@ int refined_solve(RefineArgs& ra) {
   k_c128_to_c64<<<grid_for((int64_t)n2 * n), 256, 0, st>>>(H0, n2, Mf, n2, n2, n);
   ZQ_LAUNCH_CHECK();
   ZQ_CUDA(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
-  TridiagView<float> vf = tridiag_bind<float>(tri_ws, Mf, n, n2, 64, d, e, tau);
+  TridiagView<float> vf = tridiag_bind<float>(tri_ws, Mf, n, n2, NBMAX, d, e, tau);
   vf.tc_err = tc_err;  // tensor-core products where fp32_products_on_tensor_cores allows them
   if (int rc = tridiagonalize<float>(vf, ra.nb, st)) return rc;
   if (int rc = phase_reduce(e, n, offd, phi, st)) return rc;

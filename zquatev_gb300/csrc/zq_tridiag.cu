@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   const int row = tid & (RB - 1);
   const int grp = tid >> 5;
   const int r = r0 + row;
-  __shared__ Z s_sc[4 * 64];        // per i: ya_i[j], yb_i[j], wa_i[j], wb_i[j]
+  __shared__ Z s_sc[4 * NBMAX];     // per i: ya_i[j], yb_i[j], wa_i[j], wb_i[j]
   __shared__ Z s_red[NG][RB][2];
   __shared__ double s_red_d[2][NT / 32];
 
@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   }
   if (!do_update) return;
 
-  // scalars at row j for every previous reflector of the panel (k <= nbmax = 64 < NT)
+  // scalars at row j for every previous reflector of the panel (k <= NBMAX = 128 < NT)
   if (tid < k) {
     if (tid == k - 1) { cya = csub(cya, cscale(cwa, half_c)); cyb = csub(cyb, cscale(cwb, half_c)); }
     s_sc[4 * tid + 0] = cya; s_sc[4 * tid + 1] = cyb; s_sc[4 * tid + 2] = cwa; s_sc[4 * tid + 3] = cwb;
@@ -433,11 +433,13 @@ __global__ void __launch_bounds__(128) k_hemv(TridiagView<R> v, int p, int j, in
   const Z* A = v.M;
   const Z* B = v.M + n;
   const int r0 = j + 1;
-  __shared__ Z sA[HT * HLD], sB[HT * HLD];
+  __shared__ Z sAB[2 * HT * HLD];   // the A and B tiles (also the dot CTAs' scratch: 4 warps x 128 x 4)
+  Z* sA = sAB;
+  Z* sB = sAB + HT * HLD;
   __shared__ Z sx[2][HT], sz[2][HT];   // [0]: rows of block I, [1]: rows of block J
   __shared__ Z sout[HT][4];
   // the first ndot CTAs form the panel dot partials (they start first and run
-  // beside the tiles); sA (HT * HLD >= 4 warps x 64 x 4) is their scratch
+  // beside the tiles); sAB (2 HT HLD >= 4 warps x 128 x 4) is their scratch
   if ((int)blockIdx.x < ndot) {
     panel_dots(v, p, j, k, blockIdx.x, ndot, sA);
     return;
@@ -745,7 +747,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
   const int row = tid & (HRB - 1), grp = tid / HRB;
   const int r = r0 + blockIdx.x * HRB + row;
   __shared__ Z s_v[HRB][4];
-  __shared__ Z s_dots[4 * 64];
+  __shared__ Z s_dots[4 * NBMAX];
   __shared__ Z s_part[NSPL][4 * HRB];
   __shared__ Z s_red[HNG][HRB][2];
   __shared__ double s_redd[NT / 32];
@@ -784,6 +786,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
     }
     s_part[sp][o] = cadd(cadd(s0, s2), cadd(s1, s3));
     if (tid < 4 * k) s_dots[tid] = dt;
+    for (int q = tid + NT; q < 4 * k; q += NT) s_dots[q] = v.dots[q];  // panels wider than 64
   }
   __syncthreads();
   if (!zero_mode && tid < 4 * HRB) {

@@ -54,7 +54,7 @@ __global__ void k_tune_fill(cplx<R>* M, int n, int64_t ld, uint64_t seed) {
 template <typename R>
 int tune_nb(int n, const int* cand, int ncand, double* ms_out, int* best, cudaStream_t st) {
   const size_t mbytes = sizeof(cplx<R>) * (size_t)2 * n * n;
-  const size_t wbytes = tridiag_workspace_bytes<R>(n, 64);
+  const size_t wbytes = tridiag_workspace_bytes<R>(n, NBMAX);
   const size_t sbytes = sizeof(double) * (size_t)(6 * n + 16);
   void* mem = nullptr;
   ZQ_CUDA(cudaMallocAsync(&mem, mbytes + wbytes + sbytes + 1024 + 256, st));
@@ -65,7 +65,7 @@ int tune_nb(int n, const int* cand, int ncand, double* ms_out, int* best, cudaSt
   double* d = sm;
   double* e = sm + n;
   double* tau = sm + 5 * (size_t)n;
-  TridiagView<R> v = tridiag_bind<R>(ws, M, n, 2 * n, 64, d, e, tau);
+  TridiagView<R> v = tridiag_bind<R>(ws, M, n, 2 * n, NBMAX, d, e, tau);
   if (std::is_same<R, float>::value) {
     // time the FP32 reduction as the refined path runs it
     v.tc_err = reinterpret_cast<int*>(p + ((mbytes + 255) & ~(size_t)255) + ((wbytes + 255) & ~(size_t)255) +
@@ -110,6 +110,8 @@ struct zq_batch_plan {
   int ctas_per_sm = 0, ctas = 0;
   bool tuned = false;
   double tune_ms[4] = {0, 0, 0, 0};
+  int warp_max = -1;               // switch size of the warp variant (tuned)
+  double variant_ms[4] = {0, 0, 0, 0};
   long long extent = 0;            // complex elements of D the batch touches
   void* dev = nullptr;             // tasks | info (+ counter) | per-CTA workspace
   size_t task_bytes = 0, info_bytes = 0;
@@ -129,10 +131,13 @@ constexpr int PLAN_MAX_CPS = 4;
 void* plan_ws(zq_batch_plan* p) { return reinterpret_cast<char*>(p->dev) + p->task_bytes + p->info_bytes; }
 int* plan_info(zq_batch_plan* p) { return reinterpret_cast<int*>(reinterpret_cast<char*>(p->dev) + p->task_bytes); }
 
-int plan_launch_direct(zq_batch_plan* p, double2* D, double* E, int ctas, cudaStream_t st) {
+int plan_launch_direct(zq_batch_plan* p, double2* D, double* E, int ctas, cudaStream_t st, int wmax) {
   int* info = plan_info(p);
-  return batched_launch(p->dev, p->ntask, info + p->ntask, D, E, reinterpret_cast<double*>(plan_ws(p)), ctas, info, st);
+  return batched_launch(p->dev, p->ntask, info + p->ntask, D, E, reinterpret_cast<double*>(plan_ws(p)), ctas, info, st,
+                        wmax);
 }
+// candidates of the warp variant's switch size (0: CTA variant for every size)
+constexpr int PLAN_WMAX[4] = {0, 16, 24, 32};
 
 int plan_tune(zq_batch_plan* p, double2* D, double* E, cudaStream_t st) {
   // keep the caller's input: every candidate overwrites it
@@ -145,18 +150,36 @@ int plan_tune(zq_batch_plan* p, double2* D, double* E, cudaStream_t st) {
   ZQ_CUDA(cudaEventCreate(&e1));
   double best = 1e300;
   int rc = ZQ_OK;
+  // 1) launch shape (CTAs per SM) with the default switch size
+  const int w0 = batched_warp_max();
   for (int cps = 1; cps <= PLAN_MAX_CPS && rc == ZQ_OK; ++cps) {
     const int ctas = std::min(p->ntask, cps * p->sms);
     if (cps > 1 && ctas == std::min(p->ntask, (cps - 1) * p->sms)) break;  // no more CTAs than tasks
     if (cudaMemcpyAsync(D, save, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) { rc = ZQ_ERR_CUDA; break; }
     cudaEventRecord(e0, st);
-    rc = plan_launch_direct(p, D, E, ctas, st);
+    rc = plan_launch_direct(p, D, E, ctas, st, w0);
     cudaEventRecord(e1, st);
     if (cudaEventSynchronize(e1) != cudaSuccess) rc = ZQ_ERR_CUDA;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     p->tune_ms[cps - 1] = ms;
     if (ms < best) { best = ms; p->ctas_per_sm = cps; }
+  }
+  // 2) the per-size variant: largest order solved warp-per-matrix (the rest
+  //    one CTA per matrix), at that launch shape
+  p->warp_max = w0;
+  best = 1e300;
+  const int ctas = std::min(p->ntask, p->ctas_per_sm * p->sms);
+  for (int q = 0; q < 4 && rc == ZQ_OK; ++q) {
+    if (cudaMemcpyAsync(D, save, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) { rc = ZQ_ERR_CUDA; break; }
+    cudaEventRecord(e0, st);
+    rc = plan_launch_direct(p, D, E, ctas, st, PLAN_WMAX[q]);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = ZQ_ERR_CUDA;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    p->variant_ms[q] = ms;
+    if (ms < best) { best = ms; p->warp_max = PLAN_WMAX[q]; }
   }
   if (rc == ZQ_OK && cudaMemcpyAsync(D, save, bytes, cudaMemcpyDeviceToDevice, st) != cudaSuccess) rc = ZQ_ERR_CUDA;
   cudaFreeAsync(save, st);
@@ -171,7 +194,7 @@ int plan_capture(zq_batch_plan* p, double2* D, double* E) {
   if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
   const int ctas = std::min(p->ntask, p->ctas_per_sm * p->sms);
   ZQ_CUDA(cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal));
-  int rc = plan_launch_direct(p, D, E, ctas, p->cap);
+  int rc = plan_launch_direct(p, D, E, ctas, p->cap, p->warp_max);
   cudaGraph_t g = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(p->cap, &g);
   count_launch(-1);  // capturing ran nothing; replays are counted
@@ -196,11 +219,11 @@ int zq_autotune_nb(int n2, int precision, int* best_nb, double* ms) {
     return ZQ_ERR_ARG;
   }
   const int n = n2 / 2;
-  static const int cand[3] = {16, 32, 64};
+  static const int cand[4] = {16, 32, 64, 128};
   cudaStream_t st;
   ZQ_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   int best = 32;
-  const int rc = precision == 0 ? tune_nb<double>(n, cand, 3, ms, &best, st) : tune_nb<float>(n, cand, 3, ms, &best, st);
+  const int rc = precision == 0 ? tune_nb<double>(n, cand, 4, ms, &best, st) : tune_nb<float>(n, cand, 4, ms, &best, st);
   cudaStreamDestroy(st);
   if (rc) return rc;
   nb_table_set(precision, n, best);
@@ -214,7 +237,7 @@ int zq_tuned_nb(int n2, int precision) {
 }
 
 int zq_set_tuned_nb(int n2, int precision, int nb) {
-  if (n2 < 2 || (n2 & 1) || (precision != 0 && precision != 1) || nb < 0 || nb > 64) {
+  if (n2 < 2 || (n2 & 1) || (precision != 0 && precision != 1) || nb < 0 || nb > NBMAX) {
     set_error_message("zq_set_tuned_nb: bad arguments");
     return ZQ_ERR_ARG;
   }
@@ -272,6 +295,19 @@ zq_batch_plan* zq_batch_plan_create(int count, const int* n2s, const int* ld2s, 
     return nullptr;
   }
   return p;
+}
+
+int zq_batch_plan_variant(zq_batch_plan* p, int* warp_max_n, double* ms) {
+  if (!p) return ZQ_ERR_ARG;
+  if (warp_max_n) *warp_max_n = p->warp_max < 0 ? batched_warp_max() : p->warp_max;
+  if (ms) for (int i = 0; i < 4; ++i) ms[i] = p->variant_ms[i];
+  return ZQ_OK;
+}
+
+int zq_set_batch_warp_max(int n) {
+  if (n < -1 || n > 32) { set_error_message("zq_set_batch_warp_max: -1 (default) or 0..32"); return ZQ_ERR_ARG; }
+  batched_set_warp_max(n);
+  return ZQ_OK;
 }
 
 int zq_batch_plan_run(zq_batch_plan* p, double* dD, double* deig, void* stream) {

@@ -96,13 +96,13 @@ def stedc_device(d, e, lam, z, stream=None) -> int:
 
 # ------------------------------------------------------------------- tuning
 def autotune_nb(n2: int, precision: str = "fp64") -> tuple[int, list[float]]:
-    """Times the tridiagonalisation at order n2 for panel widths 16, 32, 64 and
+    """Times the tridiagonalisation at order n2 for panel widths 16, 32, 64, 128 and
     stores the fastest for n2's size bucket ("fp64": plain path, "fp32": the
     refined path's decomposition). Returns (best nb, [ms per candidate])."""
     import ctypes
 
     best = ctypes.c_int()
-    ms = (ctypes.c_double * 3)()
+    ms = (ctypes.c_double * 4)()
     prec = {"fp64": 0, "fp32": 1}[precision]
     _lib.check(_lib.load().zq_autotune_nb(n2, prec, ctypes.byref(best), ms), "zq_autotune_nb")
     return best.value, list(ms)
@@ -145,11 +145,14 @@ class BatchPlan:
     def shape(self) -> dict:
         import ctypes
 
-        cps, ctas = ctypes.c_int(), ctypes.c_int()
+        cps, ctas, wmax = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         ms = (ctypes.c_double * 4)()
+        vms = (ctypes.c_double * 4)()
         _lib.check(_lib.load().zq_batch_plan_shape(self._h, ctypes.byref(cps), ctypes.byref(ctas), ms),
                    "zq_batch_plan_shape")
-        return {"ctas_per_sm": cps.value, "ctas": ctas.value, "tune_ms": list(ms)}
+        _lib.check(_lib.load().zq_batch_plan_variant(self._h, ctypes.byref(wmax), vms), "zq_batch_plan_variant")
+        return {"ctas_per_sm": cps.value, "ctas": ctas.value, "tune_ms": list(ms), "warp_max_n": wmax.value,
+                "variant_ms": dict(zip((0, 16, 24, 32), list(vms)))}
 
     def close(self) -> None:
         if getattr(self, "_h", None):
