@@ -181,11 +181,22 @@ __device__ __forceinline__ int seg_of(const Tc32Args& g, int kbg) {
   while (s + 1 < g.nseg && kbg >= g.kb_first[s + 1]) ++s;
   return s;
 }
+// the segment's descriptors copied into registers: each field read at a
+// constant parameter offset, not through a run-time index into parameter
+// space (which made every element load wait on descriptor loads)
+__device__ __forceinline__ Tc32Seg seg_copy(const Tc32Args& g, int s) {
+  switch (s) {
+    case 0: return g.seg[0];
+    case 1: return g.seg[1];
+    case 2: return g.seg[2];
+    default: return g.seg[3];
+  }
+}
 
 template <bool CPLX>
 __device__ __forceinline__ void stage_load(const Tc32Args& g, int kbg, int i0, int j0, int t, TcStage<CPLX>& st) {
   const int s = seg_of(g, kbg);
-  const Tc32Seg& sg = g.seg[s];
+  const Tc32Seg sg = seg_copy(g, s);
   if (CPLX) {
     const int k0 = (kbg - g.kb_first[s]) * 16;
 #pragma unroll
@@ -197,7 +208,7 @@ __device__ __forceinline__ void stage_load(const Tc32Args& g, int kbg, int i0, i
       unit_a(sg.b, t, q, c, kq);
       const int col = j0 + c;
       const bool second = sg.b2.p != nullptr && col >= sg.nsplit;
-      const Tc32Src& bs = second ? sg.b2 : sg.b;
+      const Tc32Src bs = second ? sg.b2 : sg.b;
       const int bc = second ? col - sg.nsplit : col;
       const int bcols = second ? g.n - sg.nsplit : (sg.b2.p != nullptr ? sg.nsplit : g.n);
       ld_c2(bs, bc, bcols, k0 + 2 * kq, sg.k, st.b[q]);
@@ -221,7 +232,7 @@ __device__ __forceinline__ void stage_load(const Tc32Args& g, int kbg, int i0, i
 
 template <bool CPLX>
 __device__ __forceinline__ void stage_store(const Tc32Args& g, int kbg, int t, uint32_t sa, const TcStage<CPLX>& st) {
-  const Tc32Seg& sg = g.seg[seg_of(g, kbg)];
+  const Tc32Seg sg = seg_copy(g, seg_of(g, kbg));
   const uint32_t sah = sa, sal = sa + TC_A_BYTES, sbh = sa + 2 * TC_A_BYTES, sbl = sbh + TC_B_BYTES;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
