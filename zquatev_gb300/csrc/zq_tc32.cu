@@ -8,9 +8,16 @@
 // lo = rna(x - hi) (11 + 11 significant bits: x is represented to ~2^-22),
 // and the product is formed as hi*hi + hi*lo + lo*hi with FP32 accumulation
 // in tensor memory, at the TF32 tensor rate. The accumulation in tensor memory
-// loses more than FP32 fused multiply-adds as K grows (measured: 4.6e-6 of
-// sum |a||b| at K = 4096 against 6e-8), so the path uses it where that is
-// below what the refinement removes.
+// loses more than FP32 fused multiply-adds as K grows (measured: 7.8e-7 of
+// sum |a||b| at K = 64, 2.1e-6 at 1024, 4.6e-6 at 4096, against 2.4e-7, 6e-8
+// and 6e-8 for an FP32 GEMM), so the refined path uses it only where that stays
+// below what the refinement removes (fp32_products_on_tensor_cores).
+//
+// Throughput is bound by the producers' global loads, not by the tensor pipe:
+// 4096^3 real takes 4.35 ms (95 TFLOP/s of TF32 passes), 0.70 ms when the
+// loads are replaced by constants. Ordinary loads keep too few bytes in flight
+// per SM for this rate; TMA bulk copies into a raw staging ring would be the
+// next step.
 //
 // A CTA owns a 128-row output tile: 128 complex columns (real and imaginary
 // parts: 256 accumulator columns) or 256 real columns. Complex operands are
@@ -477,16 +484,19 @@ __global__ void k_tc32_reduce(const __grid_constant__ Tc32Args g) {
 int tc32_smem_bytes() { return TC_SMEM; }
 
 bool fp32_products_on_tensor_cores(int use) {
-  // default: the Q formation, the back-transform and the large divide-and-
-  // conquer merges; the reduction's trailing update stays on the CUDA cores
-  // (its errors enter the tridiagonal itself: with the tensor-core product the
-  // refinement no longer converged from n = 1500). ZQ_FP32_PRODUCTS=cuda: none;
-  // ZQ_TC32_USES: comma list of trail, formq, applyz, dc.
+  // default: the back-transform X Z only. Measured at n2 = 8192: with the Q
+  // formation or the divide-and-conquer merges on this kernel the first
+  // refinement step leaves a correction of 1.4-3.2e-7 (6e-8 with FP32
+  // multiply-adds), above the 1e-7 that ends the refinement, so a third step
+  // (~127 ms) is needed; with the trailing update on it the refinement does not
+  // converge from n = 1500 (its errors enter the tridiagonal itself). The
+  // back-transform on it converges in two steps as before.
+  // ZQ_FP32_PRODUCTS=cuda: none; ZQ_TC32_USES: comma list of trail, formq, applyz, dc.
   static const unsigned mask = [] {
     const char* e = getenv("ZQ_FP32_PRODUCTS");
     if (e && !strcmp(e, "cuda")) return 0u;
     const char* u = getenv("ZQ_TC32_USES");
-    if (!u) return (1u << TC_USE_FORMQ) | (1u << TC_USE_APPLYZ) | (1u << TC_USE_DC);
+    if (!u) return 1u << TC_USE_APPLYZ;
     unsigned m = 0;
     if (strstr(u, "trail")) m |= 1u << TC_USE_TRAIL;
     if (strstr(u, "formq")) m |= 1u << TC_USE_FORMQ;
