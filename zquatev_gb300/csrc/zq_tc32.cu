@@ -13,11 +13,13 @@
 // and 6e-8 for an FP32 GEMM), so the refined path uses it only where that stays
 // below what the refinement removes (fp32_products_on_tensor_cores).
 //
-// Throughput is bound by the producers' global loads, not by the tensor pipe:
-// 4096^3 real takes 4.35 ms (95 TFLOP/s of TF32 passes), 0.70 ms when the
-// loads are replaced by constants. Ordinary loads keep too few bytes in flight
-// per SM for this rate; TMA bulk copies into a raw staging ring would be the
-// next step.
+// Throughput: 4096^3 real in 1.83 ms (225 TFLOP/s of TF32 passes; 0.70 ms with
+// the loads replaced by constants, so the producers' global loads still bound
+// it), the n2 = 8192 back-transform in 5.9 ms against 17 ms with FP32
+// multiply-adds. The producers' loads are unconditional and their values are
+// not touched before the stores (see ld_chunk): with per-element arithmetic
+// and bounds branches around them every load waited for the previous one
+// (4.35 ms for the same product).
 //
 // A CTA owns a 128-row output tile: 128 complex columns (real and imaginary
 // parts: 256 accumulator columns) or 256 real columns. Complex operands are
@@ -131,50 +133,63 @@ __device__ __forceinline__ uint32_t swz(int r, int c) {
   return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
 }
 
-// element (r, k) of one operand source, zero outside [0, rows) x [0, kdim);
-// the operands are not written while the kernel runs: read-only loads
-__device__ __forceinline__ float2 ld_c(const Tc32Src& s, int r, int rows, int k, int kdim) {
-  if (r >= rows || k >= kdim) return make_float2(0.f, 0.f);
-  const float2* p = reinterpret_cast<const float2*>(s.p);
-  float2 v = __ldg(s.kfast ? p + k + (int64_t)r * s.ld : p + r + (int64_t)k * s.ld);
-  if (s.conj) v.y = -v.y;
-  v.x *= s.sign; v.y *= s.sign;
-  return v;
-}
-__device__ __forceinline__ float ld_r(const Tc32Src& s, int r, int rows, int k, int kdim) {
-  if (r >= rows || k >= kdim) return 0.f;
-  return __ldg(s.kfast ? s.p + k + (int64_t)r * s.ld : s.p + r + (int64_t)k * s.ld) * s.sign;
-}
-// elements (r, k) and (r, k + 1) (k even): one 16-byte load where the source is
-// K-contiguous and aligned (vec)
-__device__ __forceinline__ void ld_c2(const Tc32Src& s, int r, int rows, int k, int kdim, float (&v)[4]) {
-  if (s.vec && r < rows && k + 1 < kdim) {
-    const float4 q = __ldg(reinterpret_cast<const float4*>(s.p + 2 * (k + (int64_t)r * s.ld)));
-    const float si = s.conj ? -s.sign : s.sign;
-    v[0] = q.x * s.sign; v[1] = q.y * si; v[2] = q.z * s.sign; v[3] = q.w * si;
-  } else {
-    const float2 a = ld_c(s, r, rows, k, kdim), b = ld_c(s, r, rows, k + 1, kdim);
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+// Raw loads of one 16-byte chunk (four floats: two complex or four real
+// elements along K) of one operand row. The loads are unconditional and their
+// values untouched here: an element outside [0, rows) x [0, kdim) reads the
+// operand's base address instead and is cleared by its mask bit later, and
+// signs / conjugation are applied when the chunk is stored. So all of a
+// thread's loads of a K block are in flight together; an arithmetic use right
+// after each load (or a branch around it) would make every load wait for the
+// previous one.
+__device__ __forceinline__ uint32_t ld_chunk(const Tc32Src& s, bool cplx, int r, int rows, int k, int kdim, float (&v)[4]) {
+  const int per = cplx ? 2 : 4;        // elements in the chunk
+  const bool row_ok = r < rows;
+  if (s.vec && row_ok && k + per - 1 < kdim) {
+    const int64_t off = cplx ? 2 * (k + (int64_t)r * s.ld) : (k + (int64_t)r * s.ld);
+    const float4 q = __ldg(reinterpret_cast<const float4*>(s.p + off));
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    return 0xFu;
   }
-}
-// elements (r, k .. k + 3) (k a multiple of 4)
-__device__ __forceinline__ void ld_r4(const Tc32Src& s, int r, int rows, int k, int kdim, float (&v)[4]) {
-  if (s.vec && r < rows && k + 3 < kdim) {
-    const float4 q = __ldg(reinterpret_cast<const float4*>(s.p + k + (int64_t)r * s.ld));
-    v[0] = q.x * s.sign; v[1] = q.y * s.sign; v[2] = q.z * s.sign; v[3] = q.w * s.sign;
+  uint32_t mask = 0;
+  if (cplx) {
+    const float2* p = reinterpret_cast<const float2*>(s.p);
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const bool ok = row_ok && k + e < kdim;
+      const float2* a = ok ? (s.kfast ? p + (k + e) + (int64_t)r * s.ld : p + r + (int64_t)(k + e) * s.ld) : p;
+      const float2 x = __ldg(a);
+      v[2 * e] = x.x; v[2 * e + 1] = x.y;
+      mask |= ok ? (3u << (2 * e)) : 0u;
+    }
   } else {
 #pragma unroll
-    for (int e = 0; e < 4; ++e) v[e] = ld_r(s, r, rows, k + e, kdim);
+    for (int e = 0; e < 4; ++e) {
+      const bool ok = row_ok && k + e < kdim;
+      const float* a = ok ? (s.kfast ? s.p + (k + e) + (int64_t)r * s.ld : s.p + r + (int64_t)(k + e) * s.ld) : s.p;
+      v[e] = __ldg(a);
+      mask |= ok ? (1u << e) : 0u;
+    }
+  }
+  return mask;
+}
+// the chunk's values as the product uses them: masked, signed, conjugated
+__device__ __forceinline__ void fix_chunk(const Tc32Src& s, bool cplx, uint32_t mask, const float (&v)[4], float (&o)[4]) {
+  const float si = (cplx && s.conj) ? -s.sign : s.sign;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const float sg = (cplx && (e & 1)) ? si : s.sign;
+    o[e] = ((mask >> e) & 1u) ? v[e] * sg : 0.f;
   }
 }
 
 // One producer thread's share of one K block, held in registers between its
-// global loads and its shared-memory stores (complex: 4 A and 4 B pairs of
-// elements; real: 4 A and 8 B quads).
+// global loads and its shared-memory stores (complex: 4 A and 4 B chunks;
+// real: 4 A and 8 B chunks), with the chunks' mask bits.
 template <bool CPLX>
 struct TcStage {
   float a[4][4];
   float b[CPLX ? 4 : 8][4];
+  uint32_t am, bm;
 };
 
 // unit q of thread t -> (row, 16-byte chunk): K-contiguous sources put eight
@@ -183,14 +198,17 @@ struct TcStage {
 __device__ __forceinline__ void unit_a(const Tc32Src& s, int t, int q, int& r, int& c) {
   if (s.kfast) { c = t & 7; r = (t >> 3) + 32 * q; } else { r = t & 127; c = (t >> 7) + 2 * q; }
 }
+__device__ __forceinline__ void unit_b(const Tc32Src& s, bool cplx, int t, int q, int& r, int& c) {
+  if (cplx || s.kfast) unit_a(s, t, q, r, c);
+  else { r = t; c = q; }
+}
 __device__ __forceinline__ int seg_of(const Tc32Args& g, int kbg) {
   int s = 0;
   while (s + 1 < g.nseg && kbg >= g.kb_first[s + 1]) ++s;
   return s;
 }
 // the segment's descriptors copied into registers: each field read at a
-// constant parameter offset, not through a run-time index into parameter
-// space (which made every element load wait on descriptor loads)
+// constant parameter offset, not through a run-time index into parameter space
 __device__ __forceinline__ Tc32Seg seg_copy(const Tc32Args& g, int s) {
   switch (s) {
     case 0: return g.seg[0];
@@ -199,72 +217,68 @@ __device__ __forceinline__ Tc32Seg seg_copy(const Tc32Args& g, int s) {
     default: return g.seg[3];
   }
 }
+// the B source of output column col (the second source past nsplit)
+__device__ __forceinline__ void b_source(const Tc32Seg& sg, int n, int col, Tc32Src& bs, int& bc, int& bcols) {
+  const bool second = sg.b2.p != nullptr && col >= sg.nsplit;
+  bs = second ? sg.b2 : sg.b;
+  bc = second ? col - sg.nsplit : col;
+  bcols = second ? n - sg.nsplit : (sg.b2.p != nullptr ? sg.nsplit : n);
+}
 
 template <bool CPLX>
 __device__ __forceinline__ void stage_load(const Tc32Args& g, int kbg, int i0, int j0, int t, TcStage<CPLX>& st) {
   const int s = seg_of(g, kbg);
   const Tc32Seg sg = seg_copy(g, s);
-  if (CPLX) {
-    const int k0 = (kbg - g.kb_first[s]) * 16;
+  const int k0 = (kbg - g.kb_first[s]) * (CPLX ? 16 : 32);
+  const int kw = CPLX ? 2 : 4;  // K elements per chunk
+  st.am = 0; st.bm = 0;
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int r, kp;
-      unit_a(sg.a, t, q, r, kp);
-      ld_c2(sg.a, i0 + r, g.m, k0 + 2 * kp, sg.k, st.a[q]);
-      int c, kq;
-      unit_a(sg.b, t, q, c, kq);
-      const int col = j0 + c;
-      const bool second = sg.b2.p != nullptr && col >= sg.nsplit;
-      const Tc32Src bs = second ? sg.b2 : sg.b;
-      const int bc = second ? col - sg.nsplit : col;
-      const int bcols = second ? g.n - sg.nsplit : (sg.b2.p != nullptr ? sg.nsplit : g.n);
-      ld_c2(bs, bc, bcols, k0 + 2 * kq, sg.k, st.b[q]);
-    }
-  } else {
-    const int k0 = (kbg - g.kb_first[s]) * 32;
+  for (int q = 0; q < 4; ++q) {
+    int r, c;
+    unit_a(sg.a, t, q, r, c);
+    st.am |= ld_chunk(sg.a, CPLX, i0 + r, g.m, k0 + kw * c, sg.k, st.a[q]) << (4 * q);
+  }
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int r, c;
-      unit_a(sg.a, t, q, r, c);
-      ld_r4(sg.a, i0 + r, g.m, k0 + 4 * c, sg.k, st.a[q]);
-    }
-#pragma unroll
-    for (int q = 0; q < (CPLX ? 4 : 8); ++q) {
-      int r, c;
-      if (sg.b.kfast) { c = t & 7; r = (t >> 3) + 32 * q; } else { r = t; c = q; }
-      ld_r4(sg.b, j0 + r, g.n, k0 + 4 * c, sg.k, st.b[q]);
-    }
+  for (int q = 0; q < (CPLX ? 4 : 8); ++q) {
+    int r, c;
+    unit_b(sg.b, CPLX, t, q, r, c);
+    Tc32Src bs;
+    int bc, bcols;
+    b_source(sg, g.n, j0 + r, bs, bc, bcols);
+    st.bm |= ld_chunk(bs, CPLX, bc, bcols, k0 + kw * c, sg.k, st.b[q]) << (4 * q);
   }
 }
 
 template <bool CPLX>
-__device__ __forceinline__ void stage_store(const Tc32Args& g, int kbg, int t, uint32_t sa, const TcStage<CPLX>& st) {
+__device__ __forceinline__ void stage_store(const Tc32Args& g, int kbg, int j0, int t, uint32_t sa,
+                                            const TcStage<CPLX>& st) {
   const Tc32Seg sg = seg_copy(g, seg_of(g, kbg));
   const uint32_t sah = sa, sal = sa + TC_A_BYTES, sbh = sa + 2 * TC_A_BYTES, sbl = sbh + TC_B_BYTES;
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     int r, c;
     unit_a(sg.a, t, q, r, c);
+    float v[4];
+    fix_chunk(sg.a, CPLX, (st.am >> (4 * q)) & 0xFu, st.a[q], v);
     const uint32_t o = swz(r, c);
-    split_store(sah + o, sal + o, st.a[q][0], st.a[q][1], st.a[q][2], st.a[q][3]);
+    split_store(sah + o, sal + o, v[0], v[1], v[2], v[3]);
   }
-  if (CPLX) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int c, kq;
-      unit_a(sg.b, t, q, c, kq);
-      const uint32_t ore = swz(c, kq), oim = swz(128 + c, kq);
-      const float* b = st.b[q];  // (re0, im0, re1, im1)
+  for (int q = 0; q < (CPLX ? 4 : 8); ++q) {
+    int r, c;
+    unit_b(sg.b, CPLX, t, q, r, c);
+    Tc32Src bs;
+    int bc, bcols;
+    b_source(sg, g.n, j0 + r, bs, bc, bcols);
+    float b[4];
+    fix_chunk(bs, CPLX, (st.bm >> (4 * q)) & 0xFu, st.b[q], b);
+    if (CPLX) {  // (re0, im0, re1, im1) -> real-part row (re, -im), imaginary-part row (im, re)
+      const uint32_t ore = swz(r, c), oim = swz(128 + r, c);
       split_store(sbh + ore, sbl + ore, b[0], -b[1], b[2], -b[3]);
       split_store(sbh + oim, sbl + oim, b[1], b[0], b[3], b[2]);
-    }
-  } else {
-#pragma unroll
-    for (int q = 0; q < (CPLX ? 4 : 8); ++q) {
-      int r, c;
-      if (sg.b.kfast) { c = t & 7; r = (t >> 3) + 32 * q; } else { r = t; c = q; }
+    } else {
       const uint32_t o = swz(r, c);
-      split_store(sbh + o, sbl + o, st.b[q][0], st.b[q][1], st.b[q][2], st.b[q][3]);
+      split_store(sbh + o, sbl + o, b[0], b[1], b[2], b[3]);
     }
   }
 }
@@ -351,7 +365,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc32(const __grid_constant__ 
       if (it + 1 < nblk) stage_load<CPLX>(g, kb0 + it + 1, i0, j0, t, nxt);
       const int stage = it % TC_STAGES, round = it / TC_STAGES;
       if (!__all_sync(0xffffffffu, mbar_wait(empty0 + 8 * stage, (round & 1) ^ 1, abort, g.wait))) { go = false; return; }
-      stage_store<CPLX>(g, kb0 + it, t, ring + stage * TC_STAGE_BYTES, cur);
+      stage_store<CPLX>(g, kb0 + it, j0, t, ring + stage * TC_STAGE_BYTES, cur);
       // generic-proxy stores become visible to the tensor core (async proxy)
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
@@ -485,12 +499,13 @@ int tc32_smem_bytes() { return TC_SMEM; }
 
 bool fp32_products_on_tensor_cores(int use) {
   // default: the back-transform X Z only. Measured at n2 = 8192: with the Q
-  // formation or the divide-and-conquer merges on this kernel the first
-  // refinement step leaves a correction of 1.4-3.2e-7 (6e-8 with FP32
-  // multiply-adds), above the 1e-7 that ends the refinement, so a third step
-  // (~127 ms) is needed; with the trailing update on it the refinement does not
-  // converge from n = 1500 (its errors enter the tridiagonal itself). The
-  // back-transform on it converges in two steps as before.
+  // formation and the divide-and-conquer merges on this kernel too, the FP32
+  // decomposition ends 30 ms earlier, but the first refinement step leaves a
+  // correction of 1.4-3.2e-7 (6e-8 with FP32 multiply-adds), above the 1e-7
+  // that ends the refinement, so a third step (~127 ms) is needed; with the
+  // trailing update on it the refinement does not converge from n = 1500 (its
+  // errors enter the tridiagonal itself). The back-transform on it converges in
+  // two steps as before.
   // ZQ_FP32_PRODUCTS=cuda: none; ZQ_TC32_USES: comma list of trail, formq, applyz, dc.
   static const unsigned mask = [] {
     const char* e = getenv("ZQ_FP32_PRODUCTS");
