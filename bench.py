@@ -763,7 +763,7 @@ def main():
     tuned_nb = {}
     for prec in ("fp32", "fp64"):
         best, ms = solver.autotune_nb(n2, prec)
-        tuned_nb[prec] = {"nb": best, "candidates": {str(c): round(m, 2) for c, m in zip((16, 32, 64), ms)}}
+        tuned_nb[prec] = {"nb": best, "candidates": {str(c): round(m, 2) for c, m in zip((16, 32, 64, 128), ms)}}
 
     for _ in range(args.warmup):
         step()
@@ -897,7 +897,7 @@ def main():
                     "d2h_bytes_per_step": n2 * n2 * 16 + n * 8, "host_memory": "pinned",
                     "samples_ms": [round(x, 1) for x in e2e_ms]},
             "gpu_launches": None,
-            "roofline": {"bound": "tensor", "kernel": "k_oz_umma (bf16 tcgen05.mma, TMEM accumulators, TMA; Ozaki slices)",
+            "roofline": {"bound": "tensor", "kernel": "k_oz_umma<2> (bf16 2-SM tcgen05.mma cta_group::2, M=256 N=256 per CTA pair; TMEM accumulators; TMA; Ozaki slices)",
                          "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": (achieved / bf16_peak) if achieved else None,
                          "traffic": (OZ_BYTES_PER_FLOP * oz_flops / oz_launches

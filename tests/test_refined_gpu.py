@@ -41,13 +41,15 @@ def test_refined_random(gpu, n, mode):
     assert np.all(np.diff(eig[:n]) >= 0)
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 2], ids=["mma_sync", "tcgen05", "tcgen05_multicast"])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3], ids=["mma_sync", "tcgen05", "tcgen05_multicast", "tcgen05_2sm"])
 @pytest.mark.parametrize("opa,opb,m,n,k", [(2, 0, 70, 50, 300), (1, 0, 70, 50, 300), (0, 0, 70, 50, 300),
-                                           (0, 3, 70, 50, 300), (0, 0, 128, 128, 32), (2, 0, 300, 260, 700)])
+                                           (0, 3, 70, 50, 300), (0, 0, 128, 128, 32), (2, 0, 300, 260, 700),
+                                           (0, 0, 130, 140, 5000)])
 def test_accurate_zgemm(gpu, kernel, opa, opb, m, n, k):
     """The Ozaki tensor-core product (either kernel) agrees with an extended-precision product to ~1e-15 relative."""
     import torch
 
+    default = gpu.zq_get_ozaki_kernel()
     assert gpu.zq_set_ozaki_kernel(kernel) == 0
     rng = np.random.default_rng(opa * 10 + opb + m)
     ash = (k, m) if opa in (1, 2) else (m, k)
@@ -68,23 +70,26 @@ def test_accurate_zgemm(gpu, kernel, opa, opb, m, n, k):
     torch.cuda.synchronize()
     assert rc == 0, _lib.last_error()
     c = dc.cpu().numpy().T
-    gpu.zq_set_ozaki_kernel(1)
+    gpu.zq_set_ozaki_kernel(default)
     scale = np.abs(op(a, opa)) @ np.abs(op(b, opb))
     err = np.abs(c - exact.astype(np.complex128)) / scale
     assert err.max() < 2e-15
 
 
+@pytest.mark.parametrize("kernel", [2, 3], ids=["multicast", "2sm"])
 @pytest.mark.parametrize("n", [64, 300, 700])
-def test_refined_multicast_products(gpu, n):
-    """The refined path with its Ozaki products on the two-CTA multicast
-    kernel (lower-triangle and full-tile launches, odd tile counts that leave a
-    tile past the matrix in the last cluster) meets the same bar."""
-    assert gpu.zq_set_ozaki_kernel(2) == 0
+def test_refined_cluster_products(gpu, n, kernel):
+    """The refined path with its Ozaki products on the two-CTA cluster kernels
+    (B shared by multicast, or 2-SM MMAs) — lower-triangle and full-tile
+    launches, odd tile counts that leave a tile past the matrix in the last
+    cluster — meets the same bar."""
+    default = gpu.zq_get_ozaki_kernel()
+    assert gpu.zq_set_ozaki_kernel(kernel) == 0
     try:
         d = inputs.random_matrix(n, 6300 + n)
         out, eig = refined(gpu, d, 1)
     finally:
-        gpu.zq_set_ozaki_kernel(1)
+        gpu.zq_set_ozaki_kernel(default)
     h = inputs.full_from_blocks(d[:n, :n], d[n:, :n])
     ref = np.linalg.eigvalsh(h)[::2]
     hn = metrics.h_norm2(ref)
@@ -96,9 +101,10 @@ def test_refined_multicast_products(gpu, n):
 
 @pytest.fixture
 def mma_sync(gpu):
+    default = gpu.zq_get_ozaki_kernel()
     assert gpu.zq_set_ozaki_kernel(0) == 0
     yield gpu
-    gpu.zq_set_ozaki_kernel(1)
+    gpu.zq_set_ozaki_kernel(default)
 
 
 @pytest.mark.parametrize("n", [5, 64, 300, 700])
@@ -157,6 +163,7 @@ def test_pipeline_wait_timeout_reports_and_recovers(gpu):
     default limit is correct."""
     import torch
 
+    default = gpu.zq_get_ozaki_kernel()
     assert gpu.zq_set_ozaki_kernel(1) == 0
     try:
         assert gpu.zq_set_pipeline_wait(300) == 0
@@ -166,7 +173,10 @@ def test_pipeline_wait_timeout_reports_and_recovers(gpu):
     finally:
         gpu.zq_set_pipeline_wait(0)
     assert float(torch.ones(1024, device="cuda").sum()) == 1024.0  # the context still answers
-    rc, a, b, c = _accurate_product(gpu, 256, 256, 256, 5)
+    try:
+        rc, a, b, c = _accurate_product(gpu, 256, 256, 256, 5)
+    finally:
+        gpu.zq_set_ozaki_kernel(default)
     assert rc == 0, _lib.last_error()
     exact = a.astype(np.clongdouble) @ b.astype(np.clongdouble)
     err = np.abs(c - exact.astype(np.complex128)) / (np.abs(a) @ np.abs(b))

@@ -198,7 +198,9 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
   using Args = ZgemmArgsT<R>;
   if (n <= 0) return ZQ_OK;
   // FP32 path: the two large products per block on the tensor cores
-  const bool use_tc = std::is_same<R, float>::value && tc_err != nullptr && fp32_products_on_tensor_cores(TC_USE_FORMQ);
+  const bool fp32 = std::is_same<R, float>::value && tc_err != nullptr;
+  const bool use_tc = fp32 && fp32_products_on_tensor_cores(TC_USE_FORMQ);     // C1 = W^H X (inner L)
+  const bool use_tc_x = fp32 && fp32_products_on_tensor_cores(TC_USE_FORMQ_X); // X -= W C2 (inner nbq)
   k_init_x<Z><<<ceil_div(2 * n * n, 256) > 4096 ? 4096 : ceil_div(2 * n * n, 256), 256, 0, st>>>(X, ldx, n, phi);
   ZQ_LAUNCH_CHECK();
   const int nref = n - 2;  // reflectors exist for columns 0..n-3
@@ -305,7 +307,7 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
     g.A1 = Tb; g.A2 = Ta; g.s2 = (R)1; g.C = C2o;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
     // Xa_sub -= Wa C2e - conj(Wb) C2o ; Xb_sub -= Wb C2e + conj(Wa) C2o   (L x L)
-    if (use_tc) {
+    if (use_tc_x) {
       if constexpr (std::is_same<R, float>::value) {
         for (int half = 0; half < 2; ++half) {
           Tc32Args t{};

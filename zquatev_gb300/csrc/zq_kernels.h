@@ -148,7 +148,11 @@ int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<
             DgemmDescT<R>* dev_desc, cudaStream_t st, int* tc_err = nullptr);
 // FP32 products of the refined path's decomposition on the tensor cores or the
 // CUDA cores, per use (environment ZQ_FP32_PRODUCTS=cuda, ZQ_TC32_USES)
-enum { TC_USE_TRAIL = 0, TC_USE_FORMQ = 1, TC_USE_APPLYZ = 2, TC_USE_DC = 3 };
+// FP32 products of the refined decomposition that may run on the TF32x3
+// tensor-core kernel: trailing update, Q formation (the W^H X products with
+// inner dimension L, and the X updates with inner dimension nbq), back-transform,
+// divide-and-conquer merges
+enum { TC_USE_TRAIL = 0, TC_USE_FORMQ = 1, TC_USE_APPLYZ = 2, TC_USE_DC = 3, TC_USE_FORMQ_X = 4 };
 bool fp32_products_on_tensor_cores(int use);
 // right half of the n2 x n2 output from the left half (U; V)
 int symmetry_fill(double2* D, int64_t ld, int n, cudaStream_t st);

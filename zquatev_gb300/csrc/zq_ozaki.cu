@@ -448,25 +448,28 @@ __global__ void __launch_bounds__(OZ_THREADS, 3) k_oz_gemm(OzGemmArgs g) {
 
 static int64_t rup(int64_t a, int64_t b) { return (a + b - 1) / b * b; }
 
-// product kernel: 0 mma.sync (k_oz_gemm), 1 tcgen05 (k_oz_umma), 2 tcgen05 in
-// two-CTA clusters sharing B by multicast (k_oz_umma<true>)
-static std::atomic<int> g_oz_kernel{1};
+// product kernel: 0 mma.sync (k_oz_gemm), 1 tcgen05 (k_oz_umma, one CTA per
+// tile), 2 tcgen05 in two-CTA clusters sharing B by multicast, 3 tcgen05 2-SM
+// MMAs on two-CTA clusters (the default: n2 = 8192 solve 422 ms against 430
+// ms with one CTA per tile and 440 ms with multicast)
+static std::atomic<int> g_oz_kernel{3};
 int ozaki_kernel() {
   if (const char* s = getenv("ZQ_OZAKI")) {
     if (!strcmp(s, "mma")) return 0;
     if (!strcmp(s, "umma")) return 1;
     if (!strcmp(s, "umma_mc")) return 2;
+    if (!strcmp(s, "umma_2sm")) return 3;
   }
   return g_oz_kernel.load();
 }
 int set_ozaki_kernel(int k) {
-  if (k < 0 || k > 2) return ZQ_ERR_ARG;
+  if (k < 0 || k > 3) return ZQ_ERR_ARG;
   g_oz_kernel.store(k);
   return ZQ_OK;
 }
 int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_bfloat16* Bis, int mp, int np, int Kp,
                  int m, int n, int nsl, int lower, const int* ea, const int* eb, double2* C, int64_t ldc, int* err,
-                 cudaStream_t st, bool multicast);
+                 cudaStream_t st, int variant);
 
 // workspace for products with m, n <= 2 * nq and Kp <= 4 * nq + 64
 size_t ozaki_workspace_bytes(int nq) {
@@ -579,7 +582,7 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
     prof_add_flops(PC_OZAKI, pairs * 2.0 * tiles * 128.0 * 128.0 * (double)Kp * 2.0);
     prof_begin(PC_OZAKI, st);
     if (int rc = oz_umma_gemm(As, Brs, Bis, (int)mp, (int)np, (int)Kp, m, n, nsl, lower ? 1 : 0, ea, eb, g.C, g.ldc, errf,
-                              st, ozaki_kernel() == 2))
+                              st, ozaki_kernel() - 1))
       return rc;
     prof_end(PC_OZAKI, st);
     int herr = 0;
@@ -626,7 +629,8 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
 
 extern "C" int zq_set_ozaki_kernel(int which) {
   if (zq::set_ozaki_kernel(which)) {
-    zq::set_error_message("kernel must be 0 (mma.sync), 1 (tcgen05) or 2 (tcgen05, cluster-multicast B)");
+    zq::set_error_message(
+        "kernel must be 0 (mma.sync), 1 (tcgen05), 2 (tcgen05, cluster-multicast B) or 3 (tcgen05 2-SM MMA)");
     return zq::ZQ_ERR_ARG;
   }
   return zq::ZQ_OK;

@@ -41,20 +41,25 @@ namespace {
 constexpr int UM_BM = 128;           // output rows per CTA (TMEM lanes)
 constexpr int UM_BN = 128;           // output columns per CTA (Re and Im: 256 accumulator columns)
 constexpr int UM_BK = 64;            // K per stage: one 128-byte swizzle row of bf16
-constexpr int UM_STAGES = 4;
 constexpr int UM_CH = 512;           // K terms per exact FP32 accumulation (512 * 127^2 < 2^24)
 constexpr int UM_SUPER = 64 * 1024;  // K terms per int32 partial (65536 * 127^2 < 2^31)
 constexpr int UM_BETA = 7;
 constexpr int UM_THREADS = 320;
 constexpr int UM_GROUP = 16;          // row tiles per group of the full-tile launch order
+constexpr int UM_EPI = 4;             // C columns whose previous values the epilogue loads together
 constexpr uint32_t UM_A_BYTES = UM_BM * UM_BK * 2;       // 16 KB
 constexpr uint32_t UM_BH_BYTES = UM_BN * UM_BK * 2;      // 16 KB (Bre or Bim half)
-constexpr uint32_t UM_STAGE_BYTES = UM_A_BYTES + 2 * UM_BH_BYTES;
+constexpr uint32_t UM_RING_BYTES = 4 * (UM_A_BYTES + 2 * UM_BH_BYTES);  // 192 KB of stages
 constexpr uint32_t UM_TMEM_COLS = 512;
-constexpr int UM_SMEM = 1024 + UM_STAGES * UM_STAGE_BYTES + 256;
+// 1 KB alignment slack, the ring, the barriers, and 16 KB of slack after them
+// so that every operand window an MMA descriptor of the last stage can span
+// (up to one B half past the stage in the 2-SM form) lies inside the allocation
+constexpr int UM_SMEM = 1024 + UM_RING_BYTES + 256 + 16384;
 constexpr long long UM_WAIT_CYCLES = 4000000000LL;  // default wait limit: about 2 s of SM clock
 // kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N = 256, M = 128
 constexpr uint32_t UM_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((128u >> 4) << 24);
+// the same for the 2-SM MMA: M = 256 (128 rows in each CTA of the pair)
+constexpr uint32_t UM_IDESC_PAIR = (1u << 4) | (1u << 7) | (1u << 10) | ((256u >> 3) << 17) | ((256u >> 4) << 24);
 
 struct UmArgs {
   int mp, np, Kp, m, n, nsl, lower;
@@ -119,6 +124,35 @@ __device__ __forceinline__ void umma_commit_mc(uint32_t bar, uint16_t mask) {
                "h"(mask)
                : "memory");
 }
+// address of the same shared variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
+}
+// TMA load into this CTA's shared memory whose completion is signalled on an
+// mbarrier of either CTA of the pair
+__device__ __forceinline__ void tma_2d_pair(uint32_t dst, const CUtensorMap* tm, int x, int y, uint32_t bar_cluster) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar_cluster)
+      : "memory");
+}
+__device__ __forceinline__ void umma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\ttcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(UM_IDESC_PAIR), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit_pair_mc(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                   bar),
+               "h"(mask)
+               : "memory");
+}
 __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
@@ -166,37 +200,61 @@ __device__ __forceinline__ double um_pow2i(int E) {
   return __longlong_as_double((long long)(1023 + E) << 52);
 }
 
-// MC: launched as clusters of two CTAs on vertically adjacent tiles of the
-// same column tile, which share the B operand: each CTA loads its own A box and
-// one half of B (rank 0 the real part, rank 1 the imaginary part) multicast to
-// both, so a CTA reads 32 KB per stage from L2 instead of 48 KB. A stage is
-// refilled once both CTAs' MMAs have released it (the MMA commit arrives on
-// both CTAs' empty barriers). A cluster's second tile past the last row tile is
+// Variants (template V):
+//   0  one CTA per 128 x 128 tile: A box + Bre box + Bim box per stage (48 KB),
+//      4 stages.
+//   1  clusters of two CTAs on vertically adjacent tiles of the same column
+//      tile, which share B: each CTA loads its own A box and one half of B
+//      (rank 0 Bre, rank 1 Bim) multicast to both, so a CTA reads 32 KB per
+//      stage from L2 instead of 48 KB; still 48 KB of shared memory per stage.
+//      A stage is refilled once both CTAs' MMAs have released it.
+//   2  the same pairs computed by 2-SM MMAs (tcgen05.mma.cta_group::2, M =
+//      256): each CTA stages only its own A box and one half of B (rank 0
+//      Bre, rank 1 Bim), 32 KB per stage, 6 stages; rank 0 issues the MMAs for
+//      both SMs, each SM's tensor core reads its own A rows and both halves of
+//      B, and each CTA's TMEM holds its 128 rows. Per MMA an SM writes and
+//      reads 8 KB of shared memory instead of 12 KB, the rate that limits the
+//      one-CTA form. Both CTAs' TMA loads complete on rank 0's full barrier;
+//      the MMA commits arrive on both CTAs' empty and accumulator barriers;
+//      rank 1's drain warps release an accumulator on rank 0's barrier.
+// In variants 1 and 2 a cluster's second tile past the last row tile is
 // computed but not written.
-template <bool MC>
+template <int V>
+struct UmShape {
+  static constexpr uint32_t stage_bytes = V == 2 ? UM_A_BYTES + UM_BH_BYTES : UM_A_BYTES + 2 * UM_BH_BYTES;
+  static constexpr int stages = V == 2 ? 6 : 4;
+};
+static_assert(UmShape<0>::stages * UmShape<0>::stage_bytes <= UM_RING_BYTES, "ring");
+static_assert(UmShape<2>::stages * UmShape<2>::stage_bytes <= UM_RING_BYTES, "ring");
+
+template <int V>
 __global__ void __launch_bounds__(UM_THREADS, 1)
     k_oz_umma(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmBr,
               const __grid_constant__ CUtensorMap tmBi, UmArgs g) {
+  constexpr bool PAIR = V != 0;
+  constexpr int STAGES = UmShape<V>::stages;
+  constexpr uint32_t STAGE_BYTES = UmShape<V>::stage_bytes;
   extern __shared__ __align__(1024) unsigned char um_smem_raw[];
   // 1024-byte aligned stage ring (128-byte swizzle atoms), barriers after it
   const uint32_t raw = su32(um_smem_raw);
   const uint32_t ring = (raw + 1023u) & ~1023u;
-  unsigned char* bar_area = um_smem_raw + (ring - raw) + UM_STAGES * UM_STAGE_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(bar_area);  // full[4], empty[4], accf[2], acce[2], done
-  const uint32_t full0 = su32(bars), empty0 = full0 + 8 * UM_STAGES, accf0 = empty0 + 8 * UM_STAGES,
+  unsigned char* bar_area = um_smem_raw + (ring - raw) + UM_RING_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(bar_area);  // full[S], empty[S], accf[2], acce[2], done
+  const uint32_t full0 = su32(bars), empty0 = full0 + 8 * STAGES, accf0 = empty0 + 8 * STAGES,
                  acce0 = accf0 + 16, done_bar = acce0 + 16;
   __shared__ uint32_t s_tmem;
   __shared__ int s_abort;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = PAIR ? cluster_rank() : 0u;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < UM_STAGES; ++s) {
+    for (int s = 0; s < STAGES; ++s) {
       mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, MC ? 2 : 1);
+      mbar_init(empty0 + 8 * s, V == 1 ? 2 : 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(accf0 + 8 * b, 1);
-      mbar_init(acce0 + 8 * b, 8);
+      mbar_init(acce0 + 8 * b, V == 2 ? 16 : 8);
     }
     mbar_init(done_bar, 1);
     s_abort = 0;
@@ -204,21 +262,29 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&s_tmem)),
-                 "r"(UM_TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    if (V == 2) {
+      // one warp of each CTA of the pair allocates collectively: the same
+      // columns in both SMs' tensor memory
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&s_tmem)),
+                   "r"(UM_TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&s_tmem)),
+                   "r"(UM_TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (MC) cluster_sync();  // the peer's barriers are initialised before any multicast or remote arrival
+  if (PAIR) cluster_sync();  // the peer's barriers are initialised before any multicast or remote arrival
   const uint32_t tmem = s_tmem;
   volatile int* abort = &s_abort;
-  const uint32_t rank = MC ? cluster_rank() : 0u;
 
   int bi, bj;
-  if (MC) {
+  if (PAIR) {
     const int tm = g.mp / UM_BM, tn = g.np / UM_BN;
     const int p = (int)(blockIdx.x >> 1);
     if (g.lower) {
@@ -256,35 +322,47 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
     if (lane == 0) {
       int ks = 0;
       bool ok = true;
+      // variant 2: both CTAs' copies complete on rank 0's full barrier
+      const uint32_t full_lead = V == 2 ? mapa_shared(full0, 0) : full0;
       for (int lev = 0; lev < g.nsl && ok; ++lev) {
         const int64_t total = (int64_t)(lev + 1) * Kp;
         for (int64_t kg = 0; kg < total && ok; kg += UM_BK) {
-          const int stage = ks % UM_STAGES, round = ks / UM_STAGES;
+          const int stage = ks % STAGES, round = ks / STAGES;
           if (!mbar_wait(empty0 + 8 * stage, (round & 1) ^ 1, abort, g.wait)) { ok = false; break; }
-          const uint32_t sA = ring + stage * UM_STAGE_BYTES;
+          const uint32_t sA = ring + stage * STAGE_BYTES;
           const int t = (int)(kg / Kp), kk = (int)(kg % Kp), u = lev - t;
-          mbar_expect_tx(full0 + 8 * stage, UM_STAGE_BYTES);
-          tma_2d(sA, &tmA, kk, t * g.mp + i0, full0 + 8 * stage);
-          if (MC) {
-            if (rank == 0) tma_2d_mc(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage, (uint16_t)3);
-            else tma_2d_mc(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage, (uint16_t)3);
+          if (V == 2) {
+            if (rank == 0) mbar_expect_tx(full0 + 8 * stage, 2 * STAGE_BYTES);
+            tma_2d_pair(sA, &tmA, kk, t * g.mp + i0, full_lead + 8 * stage);
+            if (rank == 0) tma_2d_pair(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full_lead + 8 * stage);
+            else tma_2d_pair(sA + UM_A_BYTES, &tmBi, kk, u * g.np + j0, full_lead + 8 * stage);
           } else {
-            tma_2d(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage);
-            tma_2d(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage);
+            mbar_expect_tx(full0 + 8 * stage, STAGE_BYTES);
+            tma_2d(sA, &tmA, kk, t * g.mp + i0, full0 + 8 * stage);
+            if (V == 1) {
+              if (rank == 0) tma_2d_mc(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage, (uint16_t)3);
+              else tma_2d_mc(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage, (uint16_t)3);
+            } else {
+              tma_2d(sA + UM_A_BYTES, &tmBr, kk, u * g.np + j0, full0 + 8 * stage);
+              tma_2d(sA + UM_A_BYTES + UM_BH_BYTES, &tmBi, kk, u * g.np + j0, full0 + 8 * stage);
+            }
           }
           ++ks;
         }
       }
       issued = ks;
       // copies in flight finish before the CTA may exit (after an abort in a
-      // cluster a stage may lack the peer's half and never complete: its own
-      // copies land within microseconds, so wait about a millisecond there)
-      for (int q = (issued > UM_STAGES ? issued - UM_STAGES : 0); q < issued; ++q)
-        mbar_drain(full0 + 8 * (q % UM_STAGES), (q / UM_STAGES) & 1, MC ? 2000000LL : UM_WAIT_CYCLES);
+      // cluster a stage may lack the peer's part and never complete: its own
+      // copies land within microseconds, so wait about a millisecond there).
+      // In variant 2 only rank 0 holds the full barriers; rank 1 is held at
+      // the final cluster barrier until rank 0 has drained them.
+      if (V != 2 || rank == 0)
+        for (int q = (issued > STAGES ? issued - STAGES : 0); q < issued; ++q)
+          mbar_drain(full0 + 8 * (q % STAGES), (q / STAGES) & 1, PAIR ? 2000000LL : UM_WAIT_CYCLES);
     }
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
+    if (lane == 0 && (V != 2 || rank == 0)) {
       int ks = 0, ci = 0;
       bool ok = true;
       for (int lev = 0; lev < g.nsl && ok; ++lev) {
@@ -298,26 +376,31 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
             tc_fence_after();
             const uint32_t d = tmem + (uint32_t)(buf * 256);
             for (int64_t kg = cb; kg < ce; kg += UM_BK) {
-              const int stage = ks % UM_STAGES, round = ks / UM_STAGES;
+              const int stage = ks % STAGES, round = ks / STAGES;
               if (!mbar_wait(full0 + 8 * stage, round & 1, abort, g.wait)) { ok = false; break; }
               tc_fence_after();
-              const uint32_t sA = ring + stage * UM_STAGE_BYTES;
+              const uint32_t sA = ring + stage * STAGE_BYTES;
               const uint64_t ad = sw128_desc(sA), bd = sw128_desc(sA + UM_A_BYTES);
 #pragma unroll
-              for (int k = 0; k < UM_BK / 16; ++k)  // 16 bf16 = 32 bytes along the swizzled row
-                umma_bf16(d, ad + 2 * k, bd + 2 * k, (kg != cb || k > 0) ? 1u : 0u);
-              if (MC) umma_commit_mc(empty0 + 8 * stage, (uint16_t)3);
+              for (int k = 0; k < UM_BK / 16; ++k) {  // 16 bf16 = 32 bytes along the swizzled row
+                if (V == 2) umma_bf16_pair(d, ad + 2 * k, bd + 2 * k, (kg != cb || k > 0) ? 1u : 0u);
+                else umma_bf16(d, ad + 2 * k, bd + 2 * k, (kg != cb || k > 0) ? 1u : 0u);
+              }
+              if (V == 2) umma_commit_pair_mc(empty0 + 8 * stage, (uint16_t)3);
+              else if (V == 1) umma_commit_mc(empty0 + 8 * stage, (uint16_t)3);
               else umma_commit(empty0 + 8 * stage);
               ++ks;
             }
             if (!ok) break;
-            umma_commit(accf0 + 8 * buf);
+            if (V == 2) umma_commit_pair_mc(accf0 + 8 * buf, (uint16_t)3);
+            else umma_commit(accf0 + 8 * buf);
             ++ci;
           }
         }
       }
       // every MMA issued has completed before TMEM is released
-      umma_commit(done_bar);
+      if (V == 2) umma_commit_pair_mc(done_bar, (uint16_t)1);
+      else umma_commit(done_bar);
       mbar_drain(done_bar, 0);
     }
   } else {
@@ -326,6 +409,8 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
     const int h = (warp - 2) >> 2;      // column half (0: j0..j0+63, 1: j0+64..j0+127)
     const int row = i0 + 32 * q + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+    // variant 2: an accumulator is free once both CTAs' drain warps released it
+    const uint32_t acce_lead = V == 2 ? mapa_shared(acce0, 0) : acce0;
     int ir[64], ii[64];
 #pragma unroll
     for (int c = 0; c < 64; ++c) { ir[c] = 0; ii[c] = 0; }
@@ -357,25 +442,41 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
           }
           tc_fence_before();
           __syncwarp();
-          if (lane == 0) mbar_arrive(acce0 + 8 * buf);
+          if (lane == 0) {
+            if (V == 2 && rank != 0) mbar_arrive_remote(acce_lead + 8 * buf);
+            else mbar_arrive(acce0 + 8 * buf);
+          }
           ++ci;
         }
         if (!ok) break;
         // C += 2^(ea_i + eb_j - BETA (lev + 2)) (ir + i ii) for this (level, super-chunk)
+        // The previous values of UM_EPI columns are loaded together before any
+        // of them is stored: in one load-add-store loop every load waits for
+        // the store before it (they may alias), which left the MMAs without a
+        // free accumulator for the length of 64 round trips (measured at
+        // n2 = 8192: 4 columns at a time take the second refinement step from
+        // 122 to 116 ms with 2-SM MMAs, from 130 to 124 ms with one CTA).
         if (row < g.m) {
 #pragma unroll
-          for (int c = 0; c < 64; ++c) {
-            const int col = j0 + 64 * h + c;
-            if (col < g.n) {
-              const int e_col = g.eb[col];
-              const double s = (e_row > -1000 && e_col > -1000) ? um_pow2i(e_row + e_col - UM_BETA * (lev + 2)) : 0.0;
-              double2* cp = g.C + row + (int64_t)col * g.ldc;
-              const double vr = s * (double)ir[c], vi = s * (double)ii[c];
-              if (sc == 0) *cp = make_double2(vr, vi);
-              else { double2 cur = *cp; cur.x += vr; cur.y += vi; *cp = cur; }
+          for (int c0 = 0; c0 < 64; c0 += UM_EPI) {
+            double2 cur[UM_EPI];  // addresses clamped into the matrix: no branch around the loads
+#pragma unroll
+            for (int c = 0; c < UM_EPI; ++c) {
+              const int col = j0 + 64 * h + c0 + c;
+              cur[c] = sc ? __ldcg(g.C + row + (int64_t)(col < g.n ? col : g.n - 1) * g.ldc) : make_double2(0.0, 0.0);
             }
-            ir[c] = 0;
-            ii[c] = 0;
+#pragma unroll
+            for (int c = 0; c < UM_EPI; ++c) {
+              const int col = j0 + 64 * h + c0 + c;
+              if (col < g.n) {
+                const int e_col = g.eb[col];
+                const double s = (e_row > -1000 && e_col > -1000) ? um_pow2i(e_row + e_col - UM_BETA * (lev + 2)) : 0.0;
+                g.C[row + (int64_t)col * g.ldc] =
+                    make_double2(cur[c].x + s * (double)ir[c0 + c], cur[c].y + s * (double)ii[c0 + c]);
+              }
+              ir[c0 + c] = 0;
+              ii[c0 + c] = 0;
+            }
           }
         } else {
 #pragma unroll
@@ -389,10 +490,17 @@ __global__ void __launch_bounds__(UM_THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+  // variant 2: both CTAs' MMAs and drains are finished before the collective release
+  if (V == 2) cluster_sync();
+  if (warp == 1) {
+    if (V == 2)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(UM_TMEM_COLS) : "memory");
+  }
   if (threadIdx.x == 0 && s_abort) atomicExch(g.err, 1);
-  // neither CTA leaves while its peer may still multicast into it or arrive on its barriers
-  if (MC) cluster_sync();
+  // neither CTA leaves while its peer may still copy into it or arrive on its barriers
+  if (PAIR) cluster_sync();
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -440,7 +548,8 @@ long long pipeline_wait_cycles() { return g_wait_cycles.load(); }
 // err: device int, zeroed here, raised by the kernel on a wait timeout.
 int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_bfloat16* Bis, int mp, int np, int Kp,
                  int m, int n, int nsl, int lower, const int* ea, const int* eb, double2* C, int64_t ldc, int* err,
-                 cudaStream_t st, bool multicast) {
+                 cudaStream_t st, int variant) {
+  if (variant < 0 || variant > 2) { set_error_message("oz_umma_gemm: variant 0..2"); return ZQ_ERR_ARG; }
   if (mp % UM_BM || np % UM_BN || Kp % UM_BK || nsl < 1) { set_error_message("oz_umma_gemm: bad padding"); return ZQ_ERR_ARG; }
   CUtensorMap ta, tbr, tbi;
   if (int rc = make_map(&ta, As, Kp, (int64_t)nsl * mp)) return rc;
@@ -452,8 +561,9 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
     ZQ_CUDA(cudaGetDevice(&dev));
     const unsigned long long bit = 1ull << (dev & 63);
     if (!(attr_set.load() & bit)) {
-      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
-      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
+      ZQ_CUDA(cudaFuncSetAttribute(k_oz_umma<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, UM_SMEM));
       attr_set.fetch_or(bit);
     }
   }
@@ -463,7 +573,7 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
   a.wait = g_wait_cycles.load();
   const int tm = mp / UM_BM, tn = np / UM_BN;
   ZQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-  if (multicast) {
+  if (variant != 0) {
     // clusters of two row-adjacent tiles (the last pair of a column may hold a tile past the matrix)
     int pairs = 0;
     if (lower) for (int col = 0; col < tm; ++col) pairs += (tm - col + 1) / 2;
@@ -480,10 +590,11 @@ int oz_umma_gemm(const __nv_bfloat16* As, const __nv_bfloat16* Brs, const __nv_b
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    ZQ_CUDA(cudaLaunchKernelEx(&cfg, k_oz_umma<true>, ta, tbr, tbi, a));
+    if (variant == 1) ZQ_CUDA(cudaLaunchKernelEx(&cfg, k_oz_umma<1>, ta, tbr, tbi, a));
+    else ZQ_CUDA(cudaLaunchKernelEx(&cfg, k_oz_umma<2>, ta, tbr, tbi, a));
   } else {
     const dim3 grid = lower ? dim3((unsigned)(tm * (tm + 1) / 2), 1) : dim3((unsigned)(tm * tn), 1);
-    k_oz_umma<false><<<grid, UM_THREADS, UM_SMEM, st>>>(ta, tbr, tbi, a);
+    k_oz_umma<0><<<grid, UM_THREADS, UM_SMEM, st>>>(ta, tbr, tbi, a);
   }
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;

@@ -43,6 +43,8 @@
 #include "zq_kernels.h"
 #include "zq_tc32.h"
 
+#include <string>
+
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -506,17 +508,28 @@ bool fp32_products_on_tensor_cores(int use) {
   // trailing update on it the refinement does not converge from n = 1500 (its
   // errors enter the tridiagonal itself). The back-transform on it converges in
   // two steps as before.
-  // ZQ_FP32_PRODUCTS=cuda: none; ZQ_TC32_USES: comma list of trail, formq, applyz, dc.
+  // ZQ_FP32_PRODUCTS=cuda: none; ZQ_TC32_USES: comma list of trail, formq
+  // (both kinds of Q-formation products), formq_w (the W^H X products),
+  // formq_x (the X updates), applyz, dc, none.
   static const unsigned mask = [] {
     const char* e = getenv("ZQ_FP32_PRODUCTS");
     if (e && !strcmp(e, "cuda")) return 0u;
     const char* u = getenv("ZQ_TC32_USES");
     if (!u) return 1u << TC_USE_APPLYZ;
     unsigned m = 0;
-    if (strstr(u, "trail")) m |= 1u << TC_USE_TRAIL;
-    if (strstr(u, "formq")) m |= 1u << TC_USE_FORMQ;
-    if (strstr(u, "applyz")) m |= 1u << TC_USE_APPLYZ;
-    if (strstr(u, "dc")) m |= 1u << TC_USE_DC;
+    std::string list(u);
+    size_t pos = 0;
+    while (pos <= list.size()) {
+      const size_t end = list.find(',', pos) == std::string::npos ? list.size() : list.find(',', pos);
+      const std::string tok = list.substr(pos, end - pos);
+      if (tok == "trail") m |= 1u << TC_USE_TRAIL;
+      else if (tok == "formq") m |= (1u << TC_USE_FORMQ) | (1u << TC_USE_FORMQ_X);
+      else if (tok == "formq_w") m |= 1u << TC_USE_FORMQ;
+      else if (tok == "formq_x") m |= 1u << TC_USE_FORMQ_X;
+      else if (tok == "applyz") m |= 1u << TC_USE_APPLYZ;
+      else if (tok == "dc") m |= 1u << TC_USE_DC;
+      pos = end + 1;
+    }
     return m;
   }();
   return (mask >> use) & 1u;
