@@ -44,8 +44,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "n2=8192 solve ms; mixed-stream solves/s, p99 ms vs plain FP64 at resid≤1e-12"
 # DRAM bytes (read + write) per executed bf16 flop of the Ozaki product kernel,
-# from one ncu capture of k_oz_umma (n2 = 4096, 8 slices: 4.284 GB / 2.63e12 flop)
-OZ_BYTES_PER_FLOP = 4.284e9 / 2.63e12
+# from one ncu capture of k_oz_umma<2> (n2 = 4096, second step's P1, 8 slices:
+# 6.264 + 1.048 GB / 4.95e12 flop)
+OZ_BYTES_PER_FLOP = 7.312e9 / 4.95e12
 
 
 def parse():

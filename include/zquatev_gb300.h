@@ -107,8 +107,9 @@ int zq_get_block_size(void);
 
 /* Tensor-core kernel of the Ozaki products in the refined path and
  * zq_zgemm_accurate: 0 = mma.sync (bf16 m16n8k16, 64 x 64 tiles), 1 = tcgen05
- * (TMEM accumulators, TMA-fed 128 x 256 MMAs; the default), 2 = tcgen05 in
- * clusters of two CTAs that share the B operand by TMA multicast. Same
+ * (TMEM accumulators, TMA-fed 128 x 256 MMAs, one CTA per tile), 2 = tcgen05 in
+ * clusters of two CTAs that share the B operand by TMA multicast, 3 = 2-SM
+ * tcgen05 MMAs (cta_group::2, 256 x 256 per CTA pair; the default). Same
  * arithmetic and results. */
 int zq_set_ozaki_kernel(int which);
 int zq_get_ozaki_kernel(void);

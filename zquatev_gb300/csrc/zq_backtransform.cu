@@ -23,6 +23,7 @@
 #include "zq_kernels.h"
 #include "zq_tc32.h"
 
+#include <cstdlib>
 #include <type_traits>
 
 namespace zq {
@@ -177,7 +178,20 @@ __global__ void __launch_bounds__(1024) k_build_t(const Z* G1, const Z* G2, int 
 }
 
 // split-K partial buffer of the Q formation (complex elements)
-static int64_t fq_pcap(int n, int nbq) { return (int64_t)16 * nbq * (n > 64 ? n : 64); }
+static int64_t fq_pcap(int n, int nbq) { return (int64_t)64 * nbq * (n > 64 ? n : 64); }
+
+// Most K blocks (16 complex terms each) per split of the tensor-core W^H X
+// product (env ZQ_FORMQ_KSPLIT; 0: only as many splits as fill the GPU). Each
+// split accumulates in tensor memory, whose FP32 sums truncate; the splits are
+// added in FP32 by the reduce. 8 blocks keep the refinement's second-step
+// correction at 6.2e-8 at n2 = 8192 (one accumulation per output: 2.6e-7).
+static int formq_kblocks_per_split() {
+  static const int v = [] {
+    const char* s = getenv("ZQ_FORMQ_KSPLIT");
+    return s ? atoi(s) : 8;
+  }();
+  return v;
+}
 
 size_t form_q_workspace_bytes(int n, int nbq) {
   // Wa, Wb (n x nbq), G1, G2, Ta, Tb (nbq^2), C1e, C1o, C2e, C2o (nbq x n), split-K partials
@@ -275,6 +289,9 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
         const int tiles = ceil_div(L, 128), kblk = 2 * ceil_div(L, 16);
         int splits = 1;
         while (tiles * splits < 2 * 152 && kblk / (2 * splits) >= 4 && (int64_t)(2 * splits) * L * 2 * kb <= pcap) splits *= 2;
+        // shorter accumulations in tensor memory, summed in FP32 by the reduce
+        if (const int per = formq_kblocks_per_split())
+          while (kblk / splits > per && (int64_t)(2 * splits) * L * 2 * kb <= pcap) splits *= 2;
         t.splits = splits;
         t.P = reinterpret_cast<float*>(Pk);
         t.err = tc_err;

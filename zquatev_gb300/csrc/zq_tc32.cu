@@ -500,14 +500,18 @@ __global__ void k_tc32_reduce(const __grid_constant__ Tc32Args g) {
 int tc32_smem_bytes() { return TC_SMEM; }
 
 bool fp32_products_on_tensor_cores(int use) {
-  // default: the back-transform X Z only. Measured at n2 = 8192: with the Q
-  // formation and the divide-and-conquer merges on this kernel too, the FP32
-  // decomposition ends 30 ms earlier, but the first refinement step leaves a
-  // correction of 1.4-3.2e-7 (6e-8 with FP32 multiply-adds), above the 1e-7
-  // that ends the refinement, so a third step (~127 ms) is needed; with the
-  // trailing update on it the refinement does not converge from n = 1500 (its
-  // errors enter the tridiagonal itself). The back-transform on it converges in
-  // two steps as before.
+  // default: the back-transform X Z and both kinds of Q-formation products.
+  // The tensor cores' FP32 accumulation truncates, so a long inner dimension
+  // loses accuracy: the W^H X products (inner L) are split along K into
+  // accumulations of at most 8 K blocks (128 terms), summed in FP32 by the
+  // split reduce. Measured at n2 = 8192 (a refinement step ends the solve when
+  // its correction is <= 1e-7): with these the second step's correction is
+  // 6.2e-8 (5.9e-8 with FP32 multiply-adds) and the solve takes two steps,
+  // 30 ms faster; with the W^H X products in one accumulation per output it is
+  // 2.6e-7 and a third step (~117 ms) is needed. With the divide-and-conquer
+  // merges on this kernel the refinement needs four steps; with the trailing
+  // update it does not converge from n = 1500 (its errors enter the
+  // tridiagonal itself).
   // ZQ_FP32_PRODUCTS=cuda: none; ZQ_TC32_USES: comma list of trail, formq
   // (both kinds of Q-formation products), formq_w (the W^H X products),
   // formq_x (the X updates), applyz, dc, none.
@@ -515,7 +519,7 @@ bool fp32_products_on_tensor_cores(int use) {
     const char* e = getenv("ZQ_FP32_PRODUCTS");
     if (e && !strcmp(e, "cuda")) return 0u;
     const char* u = getenv("ZQ_TC32_USES");
-    if (!u) return 1u << TC_USE_APPLYZ;
+    if (!u) return (1u << TC_USE_APPLYZ) | (1u << TC_USE_FORMQ) | (1u << TC_USE_FORMQ_X);
     unsigned m = 0;
     std::string list(u);
     size_t pos = 0;
