@@ -57,11 +57,11 @@ __global__ void k_dc_leaf(const DcNode* nodes, int cnt, const double* dmod, ZT* 
 }
 
 // one CTA per internal node. The merged poles (value, z, source column) are
-// staged in shared memory when the node fits (m <= scap): the deflation scan
-// is sequential (each close-pole rotation changes the next comparison) and
-// runs in one thread, so its operands must be a shared-memory load away, not
-// an L2 round trip. The scales are block reductions; the deflated list is
-// ranked from shared memory.
+// staged in shared memory when the node fits (m <= scap). Deflation runs in
+// parallel unless two kept poles are close enough to need a rotation (see the
+// fast path); then the sequential scan runs (each rotation changes the next
+// comparison) in one thread, with its operands a shared-memory load away, and
+// the deflated list is ranked from shared memory.
 constexpr int DC_SCAP = 8192;  // largest node staged in shared memory (20 bytes per pole)
 template <typename ZT>
 __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, const ZT* Zin, const double* lamin, int n,
@@ -107,8 +107,60 @@ __global__ void __launch_bounds__(256) k_dc_prepare(DcNode* nodes, DcWork w, con
   }
   const double dmax = block_max(dm, s_red);  // (its barriers also publish D, Zs, P)
   const double zmax = block_max(zm, s_red);
+  const double tol = 8.0 * DEPS * fmax(dmax, zmax);
+  // Fast path (all threads): z-deflation flags, compaction by a block scan,
+  // then the close-pole test on every consecutive pair of the kept poles with
+  // their original values. The sequential scan below changes a pole only
+  // after a test passes, and every test before the first pass sees original
+  // values: so if no pair passes here, the scan would rotate nothing and its
+  // lists are exactly these (the deflated ones already in ascending order).
+  // Any passing pair sends the node to the sequential scan.
+  {
+    const int per = (m + (int)blockDim.x - 1) / (int)blockDim.x;  // contiguous entries per thread
+    const int i0 = tid * per, i1 = (i0 + per < m) ? i0 + per : m;
+    int keep = 0;
+    for (int i = i0; i < i1; ++i) keep += !(rho2 * fabs(Zs[i]) <= tol);
+    // exclusive scan of the per-thread counts (warp shuffles, then the warps)
+    const int lane = tid & 31, wid = tid >> 5;
+    int incl = keep;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    __shared__ int s_wsum[8], s_flag;
+    if (lane == 31) s_wsum[wid] = incl;
+    if (tid == 0) s_flag = 0;
+    __syncthreads();
+    int wbase = 0;
+    for (int q = 0; q < wid; ++q) wbase += s_wsum[q];
+    int Ktot = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) Ktot += s_wsum[q];
+    int kpos = wbase + incl - keep;   // kept poles before this thread's chunk
+    int dpos = i0 - kpos;             // deflated ones before it
+    for (int i = i0; i < i1; ++i) {
+      if (!(rho2 * fabs(Zs[i]) <= tol)) {
+        w.nd_val[a + kpos] = D[i]; w.nd_z[a + kpos] = Zs[i]; w.nd_col[a + kpos] = P[i]; ++kpos;
+      } else {
+        w.df_val[a + dpos] = D[i]; w.df_col[a + dpos] = P[i];
+        w.df_sval[a + dpos] = D[i]; w.df_scol[a + dpos] = P[i]; ++dpos;
+      }
+    }
+    __syncthreads();
+    // pair test on the kept poles (k - 1, k), as the sequential scan forms it
+    for (int q = tid + 1; q < Ktot; q += blockDim.x) {
+      double sv = w.nd_z[a + q - 1], cc = w.nd_z[a + q];
+      const double tau = hypot(cc, sv);
+      cc /= tau; sv = -sv / tau;
+      const double t = w.nd_val[a + q] - w.nd_val[a + q - 1];
+      if (fabs(t * cc * sv) <= tol) s_flag = 1;
+    }
+    __syncthreads();
+    if (!s_flag) {
+      if (tid == 0) { nd.K = Ktot; nd.ndefl = m - Ktot; nd.nrot = 0; nd.rho2 = rho2; }
+      return;
+    }
+  }
   if (tid == 0) {
-    const double tol = 8.0 * DEPS * fmax(dmax, zmax);
     int K = 0, nd_ = 0, nr = 0;
     int pj = -1;
     for (int j = 0; j < m; ++j) {
