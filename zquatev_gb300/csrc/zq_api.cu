@@ -458,6 +458,7 @@ int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cu
   ra.ows = (mode == 1) ? reinterpret_cast<char*>(ra.ws) + ((rws + 255) & ~(size_t)255) : nullptr;
   ra.ows_bytes = (mode == 1) ? ozaki_workspace_bytes(n) : 0;
   ra.dc = &c->dc;
+  ra.coop = c->coop ? 1 : 0;
   ra.fdesc = reinterpret_cast<DgemmDescT<float>*>(desc1);
   ra.nb = nb_for(n, 1); ra.nbq = g_nbq; ra.mode = mode;
   ra.max_iter = 6;

@@ -40,6 +40,9 @@ struct Context {
   DcPlan dc;
   RefineBuffers rb;
   BatchBuffers bb;
+  // solves of this context may use cooperative launches (off for the
+  // server's lanes, whose solves run beside each other)
+  bool coop = true;
   std::mutex mu;
 };
 

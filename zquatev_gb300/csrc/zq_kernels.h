@@ -36,6 +36,7 @@ struct TridiagView {
   double* e;       // quaternion subdiagonal (4 doubles each, n)
   double* tau;     // 1 if reflector j exists else 0 (n)
   int* tc_err;     // FP32: tensor-core products allowed (their timeout flag); null: CUDA cores only
+  int coop;        // 1: the FP32 panels may run as one cooperative launch each (no other solve runs beside it)
 };
 
 template <typename R>
@@ -146,8 +147,6 @@ size_t form_q_workspace_bytes(int n, int nbq);
 template <typename R>
 int apply_z(const cplx<R>* X, int64_t ldx, const R* Z, int64_t ldz, int n, cplx<R>* out, int64_t ldo,
             DgemmDescT<R>* dev_desc, cudaStream_t st, int* tc_err = nullptr);
-// FP32 products of the refined path's decomposition on the tensor cores or the
-// CUDA cores, per use (environment ZQ_FP32_PRODUCTS=cuda, ZQ_TC32_USES)
 // FP32 products of the refined decomposition that may run on the TF32x3
 // tensor-core kernel: trailing update, Q formation (the W^H X products with
 // inner dimension L, and the X updates with inner dimension nbq), back-transform,
@@ -170,6 +169,7 @@ struct RefineArgs {
   double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap|
   int slices0;                 // Ozaki slices of the first step's products
   int slices_res;              // Ozaki slices of the products with the residual R = HX - X Lambda
+  int coop;                    // the FP32 reduction may use cooperative panel launches
   cudaStream_t st;
   cudaStream_t st2;            // second stream: Q formation overlaps the tridiagonal solve
   cudaEvent_t ev_fork, ev_join;

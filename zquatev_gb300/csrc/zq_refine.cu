@@ -623,6 +623,7 @@ int refined_solve(RefineArgs& ra) {
   ZQ_CUDA(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
   TridiagView<float> vf = tridiag_bind<float>(tri_ws, Mf, n, n2, NBMAX, d, e, tau);
   vf.tc_err = tc_err;  // tensor-core products where fp32_products_on_tensor_cores allows them
+  vf.coop = ra.coop;
   if (int rc = tridiagonalize<float>(vf, ra.nb, st)) return rc;
   if (int rc = phase_reduce(e, n, offd, phi, st)) return rc;
   mark(1, st);

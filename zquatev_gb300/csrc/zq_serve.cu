@@ -319,6 +319,7 @@ zq_server* zq_server_create(long long hbm_budget_bytes, int lanes, int max_batch
   for (int i = 0; ok && i < lanes; ++i) {
     Context* c = nullptr;
     ok = context_create(dev, &c) == ZQ_OK;
+    if (ok) c->coop = false;  // lanes solve beside each other: no cooperative launches
     if (ok) s->lanes.push_back(c);
   }
   for (int i = 0; ok && i < 2; ++i) {

@@ -51,12 +51,12 @@
 #include <cuda.h>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
 namespace zq {
 
 constexpr int RB = 32;        // rows per CTA for the row-parallel kernels
-constexpr int NG = 8;         // reflector groups per CTA in the row kernels (NT / RB)
 constexpr int TB = 64;        // tile edge of the trailing update
 constexpr int NT = 256;       // threads per CTA
 
@@ -68,11 +68,12 @@ constexpr int NT = 256;       // threads per CTA
 // written to scal[4] (f), scal[5..8] (f m), e[4j..4j+3] and tau[j]. The reads
 // bypass L1: the partials come from other CTAs of the running grid.
 // ----------------------------------------------------------------------------
+// The head's arithmetic (warp 0; lane 0 returns true with the results)
 template <typename R>
-__device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
+__device__ bool head_math(const TridiagView<R>& v, int j, int nnp, double& f, double (&m)[4], double (&ee)[4]) {
   const int lane = threadIdx.x;
   const int L = v.n - 1 - j;
-  if (lane >= 32 || L < 1) return;  // the last column has no subdiagonal entry
+  if (lane >= 32 || L < 1) return false;  // the last column has no subdiagonal entry
   const double qa0 = __ldcg(v.scal + 0), qa1 = __ldcg(v.scal + 1), qb0 = __ldcg(v.scal + 2), qb1 = __ldcg(v.scal + 3);
   // nu = scale * sqrt(sum of ssq_i (s_i / scale)^2), scale = max s_i: up to
   // 256 partials are loaded once into registers (one memory latency, one
@@ -104,10 +105,11 @@ __device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
   }
   sq = warp_sum(sq);
   const double nu = sc * sqrt(sq);
-  if (lane != 0) return;
+  if (lane != 0) return false;
   const double q1 = sqrt(qa0 * qa0 + qa1 * qa1 + qb0 * qb0 + qb1 * qb1);
-  double f = 0.0, m[4] = {0.0, 0.0, 0.0, 0.0};
-  double ee[4] = {qa0, qa1, qb0, qb1};   // L == 1: the entry itself is e_j
+  f = 0.0;
+  m[0] = m[1] = m[2] = m[3] = 0.0;
+  ee[0] = qa0; ee[1] = qa1; ee[2] = qb0; ee[3] = qb1;   // L == 1: the entry itself is e_j
   if (L >= 2) {
     if (nu > 0.0) {
       if (q1 > 0.0) {
@@ -124,6 +126,11 @@ __device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
       ee[0] = ee[1] = ee[2] = ee[3] = 0.0;  // x == 0: nothing to reduce
     }
   }
+  return true;
+}
+
+template <typename R>
+__device__ void head_write(const TridiagView<R>& v, int j, double f, const double (&m)[4], const double (&ee)[4]) {
   v.scal[4] = f;
   for (int q = 0; q < 4; ++q) v.scal[5 + q] = m[q] * f;
   // the same head rounded to R once (scal[12..15] as floats): the FP32 kernels
@@ -136,6 +143,12 @@ __device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
   v.tau[j] = (f > 0.0) ? 1.0 : 0.0;
 }
 
+template <typename R>
+__device__ void reflector_head(const TridiagView<R>& v, int j, int nnp) {
+  double f, m[4], ee[4];
+  if (head_math(v, j, nnp, f, m, ee)) head_write(v, j, f, m, ee);
+}
+
 // the reflector head in the kernel's precision: f, f m (4 reals), and whether
 // a reflector exists (f > 0)
 template <typename R>
@@ -143,6 +156,21 @@ struct WHead {
   R f, m[4];
   bool live;
 };
+
+// The FP32 head of column j formed by warp 0 of every CTA of the persistent
+// panel kernel from the norm partials (the same arithmetic as reflector_head,
+// so every CTA gets the same bits); CTA 0 also writes it to memory (the
+// subdiagonal entry and tau are used after the reduction). Lane 0 stores the
+// head in *out.
+__device__ void reflector_head_all(const TridiagView<float>& v, int j, int nnp, WHead<float>* out, bool write) {
+  double f, m[4], ee[4];
+  if (!head_math(v, j, nnp, f, m, ee)) return;
+  if (write) head_write(v, j, f, m, ee);
+  out->f = (float)f;
+  for (int q = 0; q < 4; ++q) out->m[q] = (float)(m[q] * f);
+  out->live = f > 0.0;
+}
+
 __device__ __forceinline__ void load_head(const TridiagView<float>& v, WHead<float>& h) {
   const float* hf = reinterpret_cast<const float*>(v.scal + 12);
   h.f = hf[0]; h.m[0] = hf[1]; h.m[1] = hf[2]; h.m[2] = hf[3]; h.m[3] = hf[4];
@@ -170,22 +198,26 @@ __device__ __forceinline__ void w_from_x(const WHead<R>& h, int r, int j, cplx<R
 // ----------------------------------------------------------------------------
 // colupd: rows [j, n) of column j
 // ----------------------------------------------------------------------------
-template <typename R>
-__global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, int k, int ncp, int do_update) {
-  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+// Row block `bid` (rows j + RB bid ..) of column j with NTH threads; writes
+// the block's norm partials npart[2 bid], npart[2 bid + 1]. Returns false when
+// do_update is 0 (only y_{k-1} finished). Used by k_colupd (one CTA per row
+// block) and by the persistent panel kernel.
+template <typename R, int NTH>
+__device__ bool colupd_block(const TridiagView<R>& v, int p, int j, int k, int ncp, int do_update, int bid) {
+  constexpr int NGR = NTH / RB;  // reflector groups
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
   Z* A = v.M;
   Z* B = v.M + n;
-  const int r0 = j + blockIdx.x * RB;
+  const int r0 = j + bid * RB;
   const int tid = threadIdx.x;
   const int row = tid & (RB - 1);
   const int grp = tid >> 5;
   const int r = r0 + row;
   __shared__ Z s_sc[4 * NBMAX];     // per i: ya_i[j], yb_i[j], wa_i[j], wb_i[j]
-  __shared__ Z s_red[NG][RB][2];
-  __shared__ double s_red_d[2][NT / 32];
+  __shared__ Z s_red[NGR][RB][2];
+  __shared__ double s_red_d[2][NTH / 32];
 
   // Every load that does not depend on c_{k-1} is issued first, so the kernel
   // waits about one memory latency instead of one per phase. Reflector i of
@@ -205,11 +237,11 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
     if (tid == k - 1) { cya = v.ga[j]; cyb = v.gb[j]; }
     else { cya = v.Ya[j + (int64_t)tid * v.ldy]; cyb = v.Yb[j + (int64_t)tid * v.ldy]; }
   }
-  // (3) this row's entries of the group's first two reflectors (i = grp, grp + NG)
+  // (3) this row's entries of the group's first two reflectors (i = grp, grp + NGR)
   Z pw[2][2], py[2][2];
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
-    const int i = grp + u * NG;
+    const int i = grp + u * NGR;
     pw[u][0] = pw[u][1] = py[u][0] = py[u][1] = czero<Z>();
     if (do_update && live && i < k) {
       pw[u][0] = A[r + (int64_t)(p + i) * ld]; pw[u][1] = B[r + (int64_t)(p + i) * ld];
@@ -223,7 +255,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   // (5) c_{k-1} = sum of the previous column's partials (deterministic order)
   double cl = 0.0;
   if (k > 0)
-    for (int i = tid; i < ncp; i += NT) cl += v.cpart[i];
+    for (int i = tid; i < ncp; i += NTH) cl += v.cpart[i];
   const double csum = (k > 0) ? block_sum(cl, s_red_d[0]) : 0.0;
   const R half_c = (R)(0.5 * csum);
 
@@ -232,9 +264,9 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
     v.Ya[r + (int64_t)(k - 1) * v.ldy] = csub(fga, cscale(fwa, half_c));
     v.Yb[r + (int64_t)(k - 1) * v.ldy] = csub(fgb, cscale(fwb, half_c));
   }
-  if (!do_update) return;
+  if (!do_update) return false;
 
-  // scalars at row j for every previous reflector of the panel (k <= NBMAX = 128 < NT)
+  // scalars at row j for every previous reflector of the panel (k < NBMAX = 128 <= NTH)
   if (tid < k) {
     if (tid == k - 1) { cya = csub(cya, cscale(cwa, half_c)); cyb = csub(cyb, cscale(cwb, half_c)); }
     s_sc[4 * tid + 0] = cya; s_sc[4 * tid + 1] = cyb; s_sc[4 * tid + 2] = cwa; s_sc[4 * tid + 3] = cwb;
@@ -252,8 +284,8 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   };
   if (live) {
     if (grp < k) contrib(grp, pw[0][0], pw[0][1], py[0][0], py[0][1]);
-    if (grp + NG < k) contrib(grp + NG, pw[1][0], pw[1][1], py[1][0], py[1][1]);
-    for (int i = grp + 2 * NG; i < k; i += NG) {  // panels wider than 16
+    if (grp + NGR < k) contrib(grp + NGR, pw[1][0], pw[1][1], py[1][0], py[1][1]);
+    for (int i = grp + 2 * NGR; i < k; i += NGR) {  // panels wider than 2 NGR
       const Z wa = A[r + (int64_t)(p + i) * ld], wb = B[r + (int64_t)(p + i) * ld];
       Z ya, yb;
       if (i == k - 1) { ya = v.ga[r]; yb = v.gb[r]; }
@@ -269,7 +301,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   Z xa = czero<Z>(), xb = czero<Z>();
   if (grp == 0 && r < n) {
     Z ta = s_red[0][row][0], tb = s_red[0][row][1];
-    for (int g2 = 1; g2 < NG; ++g2) { ta = cadd(ta, s_red[g2][row][0]); tb = cadd(tb, s_red[g2][row][1]); }
+    for (int g2 = 1; g2 < NGR; ++g2) { ta = cadd(ta, s_red[g2][row][0]); tb = cadd(tb, s_red[g2][row][1]); }
     xa = csub(x0a, ta);
     xb = csub(x0b, tb);
     A[r + (int64_t)j * ld] = xa;
@@ -293,10 +325,19 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
     ss = a0 * a0 + a1 * a1 + b0 * b0 + b1 * b1;
   }
   const double bss = block_sum(ss, s_red_d[1]);
-  __shared__ bool s_last;
   if (tid == 0) {
-    v.npart[2 * blockIdx.x + 0] = bmax;
-    v.npart[2 * blockIdx.x + 1] = bss;
+    v.npart[2 * bid + 0] = bmax;
+    v.npart[2 * bid + 1] = bss;
+  }
+  return true;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, int k, int ncp, int do_update) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+  if (!colupd_block<R, NT>(v, p, j, k, ncp, do_update, (int)blockIdx.x)) return;
+  __shared__ bool s_last;
+  if (threadIdx.x == 0) {
     __threadfence();
     s_last = atomicAdd(v.counter, 1u) == gridDim.x - 1;
   }
@@ -305,7 +346,7 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
   // every CTA's partials (and x_1) are visible: form the reflector head once
   __threadfence();
   reflector_head(v, j, gridDim.x);
-  if (tid == 0) *v.counter = 0u;
+  if (threadIdx.x == 0) *v.counter = 0u;
 }
 
 // ----------------------------------------------------------------------------
@@ -317,7 +358,8 @@ __global__ void __launch_bounds__(NT) k_colupd(TridiagView<R> v, int p, int j, i
 // ----------------------------------------------------------------------------
 constexpr int DR = 128;       // rows per dot-partial CTA
 template <typename R>
-__device__ void panel_dots(const TridiagView<R>& v, int p, int j, int k, int b, int ndot, cplx<R>* scratch) {
+__device__ void panel_dots(const TridiagView<R>& v, int p, int j, int k, int b, int ndot, cplx<R>* scratch,
+                           const WHead<R>* hd = nullptr) {
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -329,7 +371,7 @@ __device__ void panel_dots(const TridiagView<R>& v, int p, int j, int k, int b, 
   WHead<R> h;
   Z xa = czero<Z>(), xb = czero<Z>();
   if (live) {
-    load_head(v, h);
+    if (hd) h = *hd; else load_head(v, h);
     xa = A[gr + (int64_t)j * ld];
     xb = B[gr + (int64_t)j * ld];
   }
@@ -574,38 +616,34 @@ __device__ __forceinline__ float2 lds2(uint32_t a) {
   return v;
 }
 
-__global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtensorMap tm, TridiagView<float> v, int p,
-                                                  int j, int k, int ndot, int b0) {
-  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+// One work item of the TMA hemv grid with 128 threads: items < ndot are panel
+// dot partials, the others lower-triangle tiles. `tiles` is a 1024-aligned
+// 16 KB shared buffer, `bar` an initialised mbarrier whose next phase has
+// parity `par`; `hd` the reflector head when the caller holds it. Returns
+// false if the tile copy did not arrive within the wait limit.
+__device__ bool hemv_tma_item(const CUtensorMap* tmp, const TridiagView<float>& v, int p, int j, int k, int ndot, int b0,
+                              int item, uint32_t tiles, unsigned char* tiles_gen, uint32_t bar, uint32_t par,
+                              const WHead<float>* hd) {
   using Z = float2;
-  extern __shared__ __align__(1024) unsigned char hm_raw[];
-  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(hm_raw);
-  const uint32_t tiles = (raw + 1023u) & ~1023u;    // A tile at +0, B tile at +8192
-  unsigned char* tiles_gen = hm_raw + (tiles - raw);
   __shared__ float4 s_xd[2][HT], s_zd[2][HT];       // [0]: block I rows, [1]: block J rows
   __shared__ Z sout[HT][4];
-  __shared__ __align__(8) unsigned long long s_bar;
   const int n = v.n;
   const int64_t ld = v.ld;
   const Z* A = v.M;
   const Z* B = v.M + n;
-  if ((int)blockIdx.x < ndot) {
-    panel_dots(v, p, j, k, blockIdx.x, ndot, reinterpret_cast<Z*>(tiles_gen));
-    return;
+  if (item < ndot) {
+    panel_dots(v, p, j, k, item, ndot, reinterpret_cast<Z*>(tiles_gen), hd);
+    return true;
   }
-  const int t = blockIdx.x - ndot;
+  const int t = item - ndot;
   int I, J;
   tri_tile(t, I, J);
   const bool diag = (I == J);
   const int tid = threadIdx.x;
   const int rbase = b0 + I * HT, cbase = b0 + J * HT;
-  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(16384u) : "memory");
-    const uint64_t tma = reinterpret_cast<uint64_t>(&tm);
+    const uint64_t tma = reinterpret_cast<uint64_t>(tmp);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int x = (q >= 2 ? n : 0) + rbase + 16 * (q & 1);   // row: even (b0, n even)
@@ -623,7 +661,7 @@ __global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtens
     Z x = czero<Z>(), z = czero<Z>();
     if (wg > j && wg < n) {
       WHead<float> h;
-      load_head(v, h);
+      if (hd) h = *hd; else load_head(v, h);
       x = A[wg + (int64_t)j * ld];
       z = B[wg + (int64_t)j * ld];
       w_from_x<float>(h, wg, j, x, z);
@@ -639,15 +677,15 @@ __global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtens
     uint32_t ok = 0;
     while (!ok) {
       asm volatile(
-          "{\n\t.reg .pred pp;\n\tmbarrier.try_wait.parity.shared::cta.b64 pp, [%1], 0;\n\tselp.u32 %0, 1, 0, pp;\n\t}"
+          "{\n\t.reg .pred pp;\n\tmbarrier.try_wait.parity.shared::cta.b64 pp, [%1], %2;\n\tselp.u32 %0, 1, 0, pp;\n\t}"
           : "=r"(ok)
-          : "r"(bar)
+          : "r"(bar), "r"(par)
           : "memory");
       if (!ok && clock64() - t0 > 4000000000LL) break;
     }
-    if (!__all_sync(0xffffffffu, ok != 0)) {
-      if ((tid & 31) == 0 && v.tc_err) atomicExch(v.tc_err, 1);
-      return;
+    if (!__syncthreads_and(ok != 0)) {
+      if (tid == 0 && v.tc_err) atomicExch(v.tc_err, 1);
+      return false;
     }
   }
   const int role = tid >> 5, q = tid & (HT - 1);
@@ -719,7 +757,26 @@ __global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtens
     Z* o = v.hpart + (((int64_t)I * nbm + J) * HT + q) * 4 + 2 * role;
     o[0] = a0; o[1] = a1;
   }
+  return true;
 }
+
+__global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtensorMap tm, TridiagView<float> v, int p,
+                                                  int j, int k, int ndot, int b0) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+  extern __shared__ __align__(1024) unsigned char hm_raw[];
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(hm_raw);
+  const uint32_t tiles = (raw + 1023u) & ~1023u;    // A tile at +0, B tile at +8192
+  __shared__ __align__(8) unsigned long long s_bar;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+  if ((int)blockIdx.x >= ndot && threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  hemv_tma_item(&tm, v, p, j, k, ndot, b0, (int)blockIdx.x, tiles, hm_raw + (tiles - raw), bar, 0u, nullptr);
+}
+
+
 
 // ----------------------------------------------------------------------------
 // hreduce: g = H_panelstart w - corrections, for rows [j+1, n); c partials;
@@ -731,12 +788,13 @@ __global__ void __launch_bounds__(128) k_hemv_tma(const __grid_constant__ CUtens
 //   depend on one another are issued before the first is used.
 // ----------------------------------------------------------------------------
 constexpr int HRB = 8;                 // rows per CTA
-constexpr int HNG = NT / HRB;          // reflector groups for the corrections
-constexpr int NSPL = NT / (4 * HRB);   // threads per (row, product) for the tile partials
-template <typename R>
-__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode,
-                                                int sh) {
-  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+// Row block `bid` (rows j + 1 + HRB bid ..) with NTH threads; `hd` is the
+// reflector head when the caller holds it (null: read from scal).
+template <typename R, int NTH>
+__device__ void hreduce_block(const TridiagView<R>& v, int p, int j, int k, int T, int nblk, int zero_mode, int sh,
+                              int bid, const WHead<R>* hd) {
+  constexpr int HNG = NTH / HRB;          // reflector groups for the corrections
+  constexpr int NSPL = NTH / (4 * HRB);   // threads per (row, product) for the tile partials
   using Z = cplx<R>;
   const int n = v.n;
   const int64_t ld = v.ld;
@@ -745,17 +803,17 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
   const int r0 = j + 1;
   const int tid = threadIdx.x;
   const int row = tid & (HRB - 1), grp = tid / HRB;
-  const int r = r0 + blockIdx.x * HRB + row;
+  const int r = r0 + bid * HRB + row;
   __shared__ Z s_v[HRB][4];
   __shared__ Z s_dots[4 * NBMAX];
   __shared__ Z s_part[NSPL][4 * HRB];
   __shared__ Z s_red[HNG][HRB][2];
-  __shared__ double s_redd[NT / 32];
+  __shared__ double s_redd[NTH / 32];
   // this row's x and the reflector head (w = f x is written in place at the end)
   WHead<R> h;
   Z xa = czero<Z>(), xb = czero<Z>();
   if (grp == 0 && r < n) {
-    load_head(v, h);
+    if (hd) h = *hd; else load_head(v, h);
     xa = A[r + (int64_t)j * ld];
     xb = B[r + (int64_t)j * ld];
   }
@@ -769,7 +827,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
     if (tid < 4 * k) dt = v.dots[tid];
     // tile partials: output o = (row, product); split sp sums blocks S = sp, sp + NSPL, ...
     const int o = tid & (4 * HRB - 1), sp = tid / (4 * HRB);
-    const int lr = blockIdx.x * HRB + (o >> 2);
+    const int lr = bid * HRB + (o >> 2);
     Z s0 = czero<Z>(), s1 = czero<Z>(), s2 = czero<Z>(), s3 = czero<Z>();
     if (r0 + lr < n) {
       const int Rb = (lr + sh) / T, off = (lr + sh) % T;  // the hemv tile grid starts sh rows above r0
@@ -786,7 +844,7 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
     }
     s_part[sp][o] = cadd(cadd(s0, s2), cadd(s1, s3));
     if (tid < 4 * k) s_dots[tid] = dt;
-    for (int q = tid + NT; q < 4 * k; q += NT) s_dots[q] = v.dots[q];  // panels wider than 64
+    for (int q = tid + NTH; q < 4 * k; q += NTH) s_dots[q] = v.dots[q];  // wide panels
   }
   __syncthreads();
   if (!zero_mode && tid < 4 * HRB) {
@@ -833,7 +891,14 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
     v.gb[r] = gb;
   }
   const double bs = block_sum(cp, s_redd);
-  if (tid == 0) v.cpart[blockIdx.x] = bs;
+  if (tid == 0) v.cpart[bid] = bs;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, int k, int T, int nblk, int zero_mode,
+                                                int sh) {
+  pdl_wait();  // launched with launch_pdl: the previous kernel's results first
+  hreduce_block<R, NT>(v, p, j, k, T, nblk, zero_mode, sh, (int)blockIdx.x, nullptr);
 }
 
 // ----------------------------------------------------------------------------
@@ -987,6 +1052,136 @@ static int trail_tc32(const TridiagView<float>& v, int p, int nbp, int t0, cudaS
   return ZQ_OK;
 }
 
+
+// ----------------------------------------------------------------------------
+// Persistent panel kernel (FP32 with the TMA mat-vec; opt-in, ZQ_TRIDIAG=persist):
+// the columns of one panel in a single cooperative launch. Per column the
+// three phases of the kernel sequence above (colupd row blocks, hemv items,
+// hreduce row blocks) run as loops over the resident CTAs with a grid barrier
+// after each, and every CTA forms the reflector head itself after the first
+// barrier: 3 nb barriers instead of 3 nb launches. Measured slower than the
+// launches at every size (FP32 reduction at n2 = 1024 / 4096 / 8192: 12.6-14.3
+// / 64-69 / 198-265 ms with 1-6 CTAs per SM, against 11.6 / 53.2 / 156.4 ms):
+// a grid barrier costs about what a dependent launch does, and a fixed grid
+// streams the mat-vec tiles more slowly than thousands of one-tile CTAs.
+// ----------------------------------------------------------------------------
+constexpr int PT = 128;  // threads per CTA of the persistent panel kernel
+constexpr int PT_SMEM = 1024 + 16384;  // 1024-aligned 16 KB tile buffer
+
+// Grid barrier of the persistent kernel (cooperative launch: every CTA is
+// resident). counter[2] counts arrivals, counter[3] is the generation,
+// counter[4] the abort flag. A wait longer than `limit` cycles raises the
+// abort flag and tc_err, after which every barrier returns at once (false).
+__device__ bool grid_barrier(const TridiagView<float>& v, long long limit) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = v.counter + 3;
+    volatile unsigned* abt = v.counter + 4;
+    int ok = *abt == 0u;
+    if (ok) {
+      const unsigned g0 = *gen;  // read before arriving: it cannot advance until this CTA arrives
+      __threadfence();
+      if (atomicAdd(v.counter + 2, 1u) == gridDim.x - 1) {
+        atomicExch(v.counter + 2, 0u);
+        __threadfence();
+        atomicAdd(v.counter + 3, 1u);
+      } else {
+        const long long t0 = clock64();
+        while (*gen == g0) {
+          __nanosleep(64);  // back off: hundreds of CTAs poll the same line
+          if (*abt) { ok = 0; break; }
+          if (clock64() - t0 > limit) {
+            atomicExch(v.counter + 4, 1u);
+            if (v.tc_err) atomicExch(v.tc_err, 1);
+            ok = 0;
+            break;
+          }
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(PT, 4) k_panel_persist(const __grid_constant__ CUtensorMap tm, TridiagView<float> v,
+                                                      int p, int nbp, long long limit) {
+  extern __shared__ __align__(1024) unsigned char pp_raw[];
+  const uint32_t raw = (uint32_t)__cvta_generic_to_shared(pp_raw);
+  const uint32_t tiles = (raw + 1023u) & ~1023u;
+  __shared__ __align__(8) unsigned long long s_bar;
+  __shared__ WHead<float> s_head;
+  const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&s_bar);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t par = 0;  // parity of the tile barrier's next phase
+  const int n = v.n, G = (int)gridDim.x, cta = (int)blockIdx.x;
+  int ncp = 0;
+  for (int k = 0; k < nbp; ++k) {
+    const int j = p + k, L = n - 1 - j;
+    const int ncta1 = ceil_div(n - j, RB);
+    for (int rb = cta; rb < ncta1; rb += G) colupd_block<float, PT>(v, p, j, k, ncp, 1, rb);
+    if (!grid_barrier(v, limit)) return;
+    if (L < 1) { ncp = 0; continue; }
+    reflector_head_all(v, j, ncta1, &s_head, cta == 0);
+    __syncthreads();
+    const int b0 = (j + 1) & ~1, sh = (j + 1) - b0;
+    const int nblk = ceil_div(n - b0, HT);
+    if (L >= 2) {
+      const int ndot = (k > 0) ? ceil_div(L, DR) : 0;
+      const int items = ndot + nblk * (nblk + 1) / 2;
+      for (int it = cta; it < items; it += G) {
+        // the tile buffer was read by this CTA's threads (generic proxy) before
+        // the copy of this item writes it (async proxy)
+        if (threadIdx.x == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const bool ok = hemv_tma_item(&tm, v, p, j, k, ndot, b0, it, tiles, pp_raw + (tiles - raw), bar, par, &s_head);
+        if (it >= ndot) par ^= 1u;
+        __syncthreads();
+        if (!ok) {
+          if (threadIdx.x == 0) atomicExch(v.counter + 4, 1u);
+          return;
+        }
+      }
+      if (!grid_barrier(v, limit)) return;
+    }
+    const int nhr = ceil_div(L, HRB);
+    for (int rb = cta; rb < nhr; rb += G)
+      hreduce_block<float, PT>(v, p, j, k, HT, nblk, L < 2 ? 1 : 0, sh, rb, &s_head);
+    if (!grid_barrier(v, limit)) return;
+    ncp = nhr;
+  }
+}
+
+// CTAs of the persistent panel kernel (0: use the per-column kernels). Only
+// with ZQ_TRIDIAG=persist; the grid is every SM times min(occupancy,
+// ZQ_PANEL_CTAS_PER_SM, default 4).
+static int panel_persist_grid() {
+  static int grid = -1;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    grid = 0;
+    const char* m = getenv("ZQ_TRIDIAG");
+    if (!m || strcmp(m, "persist")) return;
+    int dev = 0, sms = 0, coop = 0, occ = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return;
+    if (cudaFuncSetAttribute(k_panel_persist, cudaFuncAttributeMaxDynamicSharedMemorySize, PT_SMEM) != cudaSuccess) return;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel_persist, PT, PT_SMEM) != cudaSuccess) return;
+    int per = 4;
+    if (const char* e = getenv("ZQ_PANEL_CTAS_PER_SM")) per = atoi(e);
+    if (per > occ) per = occ;
+    grid = per > 0 ? per * sms : 0;
+  });
+  return grid;
+}
+
 // ----------------------------------------------------------------------------
 // host driver
 // ----------------------------------------------------------------------------
@@ -996,7 +1191,7 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
   if (n <= 0) return ZQ_OK;
   if (nb > v.nbmax) nb = v.nbmax;
   if (nb < 1) nb = 1;
-  ZQ_CUDA(cudaMemsetAsync(v.counter, 0, 2 * sizeof(unsigned), st));
+  ZQ_CUDA(cudaMemsetAsync(v.counter, 0, 5 * sizeof(unsigned), st));
   // FP32 with even n: the hemv tiles come by TMA from one tensor map over [A; B]
   // (2n x n, 8-byte elements, 16 x 32 boxes, 128-byte swizzle, zeros outside)
   bool use_tma = false;
@@ -1016,9 +1211,28 @@ int tridiagonalize(TridiagView<R> v, int nb, cudaStream_t st) {
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
   }
   int ncp = 0;  // number of c partials of the previous column
+  const int pgrid = (use_tma && v.coop) ? panel_persist_grid() : 0;
   for (int p = 0; p < n; p += nb) {
     const int nbp = (nb < n - p) ? nb : (n - p);
-    for (int k = 0; k < nbp; ++k) {
+    if constexpr (std::is_same<R, float>::value) if (pgrid > 0) {
+      // the panel's columns in one cooperative launch
+      cudaLaunchConfig_t cfg{};
+      cfg.gridDim = dim3((unsigned)pgrid);
+      cfg.blockDim = dim3(PT);
+      cfg.dynamicSmemBytes = PT_SMEM;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      const long long limit = pipeline_wait_cycles();
+      ZQ_CUDA(cudaLaunchKernelEx(&cfg, k_panel_persist, hemv_map, v, p, nbp, limit));
+      count_launch();
+      const int jl = p + nbp - 1, Ll = n - 1 - jl;
+      ncp = Ll >= 1 ? ceil_div(Ll, HRB) : 0;
+    }
+    for (int k = 0; k < nbp && pgrid == 0; ++k) {
       const int j = p + k;
       const int L = n - 1 - j;
       const int ncta1 = ceil_div(n - j, RB);
@@ -1093,7 +1307,7 @@ size_t tridiag_workspace_bytes(int n, int nbmax) {
   b += sizeof(Z) * (4 * (size_t)nbmax);               // dots
   b += sizeof(double) * (2 * hblk + 16);              // npart (2 hblk), scal
   b += sizeof(double) * ((size_t)ceil_div(n > 0 ? n : 1, HRB) + 1);  // cpart (one per hreduce CTA)
-  b += sizeof(unsigned) * 2;                          // counters
+  b += sizeof(unsigned) * 8;                          // counters (colupd, dots, grid barrier, abort)
   return b + 16 * 256;
 }
 
@@ -1115,7 +1329,8 @@ TridiagView<R> tridiag_bind(void* ws, cplx<R>* M, int n, int64_t ld, int nbmax, 
   v.npart = reinterpret_cast<double*>(take(sizeof(double) * 2 * hblk));
   v.cpart = reinterpret_cast<double*>(take(sizeof(double) * ((size_t)ceil_div(n > 0 ? n : 1, HRB) + 1)));
   v.scal = reinterpret_cast<double*>(take(sizeof(double) * 16));
-  v.counter = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * 2));
+  v.counter = reinterpret_cast<unsigned*>(take(sizeof(unsigned) * 8));
+  v.coop = 1;
   v.d = d; v.e = e; v.tau = tau;
   return v;
 }
