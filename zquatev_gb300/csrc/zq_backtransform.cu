@@ -23,6 +23,7 @@
 #include "zq_kernels.h"
 #include "zq_tc32.h"
 
+#include <atomic>
 #include <cstdlib>
 #include <type_traits>
 
@@ -177,6 +178,53 @@ __global__ void __launch_bounds__(1024) k_build_t(const Z* G1, const Z* G2, int 
   }
 }
 
+// The same recurrence for FP32 with G1, G2, Ta, Tb in shared memory (4 kb^2
+// complex64, 128 KB at kb = 64): each step reads what the previous one wrote
+// a shared-memory load away instead of an L2 round trip.
+__global__ void __launch_bounds__(1024) k_build_t_sm(const float2* G1, const float2* G2, int kb, float2* Ta,
+                                                     float2* Tb) {
+  extern __shared__ float2 bt_sm[];
+  float2* g1 = bt_sm;
+  float2* g2 = g1 + kb * kb;
+  float2* ta_s = g2 + kb * kb;
+  float2* tb_s = ta_s + kb * kb;
+  const int tid = threadIdx.x;
+  const int i = tid & 63, g = tid >> 6;
+  __shared__ float2 red[BT_G][64][2];
+  for (int t = tid; t < kb * kb; t += blockDim.x) {
+    g1[t] = G1[t]; g2[t] = G2[t];
+    ta_s[t] = czero<float2>(); tb_s[t] = czero<float2>();
+  }
+  __syncthreads();
+  for (int k = 0; k < kb; ++k) {
+    float2 sa = czero<float2>(), sb = sa;
+    if (i < k) {
+      for (int l = i + g; l < k; l += BT_G) {
+        const float2 ta = ta_s[i + l * kb], tb = tb_s[i + l * kb];
+        const float2 a1 = g1[l + k * kb], a2 = g2[l + k * kb];
+        cfma(sa, ta, a1); cfmac(sa, cneg(tb), a2);
+        cfma(sb, tb, a1); cfmac(sb, ta, a2);
+      }
+    }
+    red[g][i][0] = sa;
+    red[g][i][1] = sb;
+    __syncthreads();
+    if (g == 0) {
+      if (i < k) {
+        float2 ta = czero<float2>(), tb = ta;
+        for (int q = 0; q < BT_G; ++q) { ta = cadd(ta, red[q][i][0]); tb = cadd(tb, red[q][i][1]); }
+        ta_s[i + k * kb] = cneg(ta);
+        tb_s[i + k * kb] = cneg(tb);
+      } else if (i == k) {
+        ta_s[k + k * kb] = make_float2(1.f, 0.f);
+        tb_s[k + k * kb] = czero<float2>();
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < kb * kb; t += blockDim.x) { Ta[t] = ta_s[t]; Tb[t] = tb_s[t]; }
+}
+
 // split-K partial buffer of the Q formation (complex elements)
 static int64_t fq_pcap(int n, int nbq) { return (int64_t)64 * nbq * (n > 64 ? n : 64); }
 
@@ -256,7 +304,20 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
     if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
     g.A1 = Wa; g.B1 = Wb; g.A2 = Wb; g.B2 = Wa; g.s2 = (R)-1; g.C = G2;
     if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
-    k_build_t<Z><<<1, 1024, 0, st>>>(G1, G2, kb, Ta, Tb);
+    if constexpr (std::is_same<R, float>::value) {
+      const size_t sm = sizeof(float2) * 4 * (size_t)kb * kb;  // kb <= 64: <= 128 KB
+      static std::atomic<unsigned long long> attr_set{0};  // per device
+      int dev = 0;
+      ZQ_CUDA(cudaGetDevice(&dev));
+      const unsigned long long bit = 1ull << (dev & 63);
+      if (!(attr_set.load() & bit)) {
+        ZQ_CUDA(cudaFuncSetAttribute(k_build_t_sm, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 64 * 64 * 8));
+        attr_set.fetch_or(bit);
+      }
+      k_build_t_sm<<<1, 1024, sm, st>>>(G1, G2, kb, Ta, Tb);
+    } else {
+      k_build_t<Z><<<1, 1024, 0, st>>>(G1, G2, kb, Ta, Tb);
+    }
     ZQ_LAUNCH_CHECK();
     // C1e = Wa^H Xa_sub + Wb^H Xb_sub ; C1o = Wa^T Xb_sub - Wb^T Xa_sub   (kb x L)
     Z* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
