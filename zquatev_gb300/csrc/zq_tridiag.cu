@@ -906,6 +906,43 @@ __global__ void __launch_bounds__(NT) k_hreduce(TridiagView<R> v, int p, int j, 
 // region [t0, n) x [t0, n), rank-4*nbp structured update.
 // ----------------------------------------------------------------------------
 constexpr int KC = 4;  // reflectors per smem stage
+__device__ __forceinline__ void cp_async8_zfill(void* smem, const void* gmem, bool pred) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(sa), "l"(gmem), "r"(pred ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// the rank-4 KC products of one K stage into the 4 x 4 complex micro-tiles
+template <typename Z>
+__device__ __forceinline__ void trail_stage(const Z (&sr)[4][KC][TB], const Z (&sc)[4][KC][TB], int tr, int tc,
+                                            Z (&accA)[4][4], Z (&accB)[4][4]) {
+#pragma unroll
+  for (int kk = 0; kk < KC; ++kk) {
+    Z rwa[4], rwb[4], rya[4], ryb[4], cwa[4], cwb[4], cya[4], cyb[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      rwa[q] = sr[0][kk][4 * tr + q]; rwb[q] = sr[1][kk][4 * tr + q];
+      rya[q] = sr[2][kk][4 * tr + q]; ryb[q] = sr[3][kk][4 * tr + q];
+      cwa[q] = sc[0][kk][4 * tc + q]; cwb[q] = sc[1][kk][4 * tc + q];
+      cya[q] = sc[2][kk][4 * tc + q]; cyb[q] = sc[3][kk][4 * tc + q];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        // A += wa conj(ya) + conj(wb) yb + ya conj(wa) + conj(yb) wb
+        cfmacb(accA[q][c], rwa[q], cya[c]); cfmac(accA[q][c], rwb[q], cyb[c]);
+        cfmacb(accA[q][c], rya[q], cwa[c]); cfmac(accA[q][c], ryb[q], cwb[c]);
+        // B += wb conj(ya) - conj(wa) yb + yb conj(wa) - conj(ya) wb
+        cfmacb(accB[q][c], rwb[q], cya[c]); cfmac(accB[q][c], cneg(rwa[q]), cyb[c]);
+        cfmacb(accB[q][c], ryb[q], cwa[c]); cfmac(accB[q][c], cneg(rya[q]), cwb[c]);
+      }
+  }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(NT) k_trail(TridiagView<R> v, int p, int nbp, int t0) {
   pdl_wait();  // launched with launch_pdl: the previous kernel's results first
@@ -920,61 +957,73 @@ __global__ void __launch_bounds__(NT) k_trail(TridiagView<R> v, int p, int nbp, 
   const int tid = threadIdx.x;
   const int tr = tid & 15, tc = tid >> 4;
   const int rb = t0 + I * TB, cb = t0 + J * TB;
-  // [vector: wa, wb, ya, yb][kk][row]
-  __shared__ Z s_r[4][KC][TB];
-  __shared__ Z s_c[4][KC][TB];
   Z accA[4][4], accB[4][4];
 #pragma unroll
   for (int q = 0; q < 4; ++q)
 #pragma unroll
     for (int c = 0; c < 4; ++c) { accA[q][c] = czero<Z>(); accB[q][c] = czero<Z>(); }
 
-  for (int k0 = 0; k0 < nbp; k0 += KC) {
-    __syncthreads();
-    for (int e = tid; e < 4 * KC * TB; e += NT) {
-      const int row = e % TB, kk = (e / TB) % KC, vec = e / (TB * KC);
-      const int kg = k0 + kk;
-      Z vr = czero<Z>(), vc = czero<Z>();
-      if (kg < nbp) {
-        const int gr = rb + row, gc = cb + row;
-        if (gr < n) {
-          if (vec == 0) vr = A[gr + (int64_t)(p + kg) * ld];
-          else if (vec == 1) vr = B[gr + (int64_t)(p + kg) * ld];
-          else if (vec == 2) vr = v.Ya[gr + (int64_t)kg * v.ldy];
-          else vr = v.Yb[gr + (int64_t)kg * v.ldy];
-        }
-        if (gc < n) {
-          if (vec == 0) vc = A[gc + (int64_t)(p + kg) * ld];
-          else if (vec == 1) vc = B[gc + (int64_t)(p + kg) * ld];
-          else if (vec == 2) vc = v.Ya[gc + (int64_t)kg * v.ldy];
-          else vc = v.Yb[gc + (int64_t)kg * v.ldy];
-        }
+  if constexpr (std::is_same<R, float>::value) {
+    // FP32: the [vector: wa, wb, ya, yb][kk][row] stages double-buffered by
+    // cp.async (zero fill outside the matrix): the next stage's copies are in
+    // flight while this stage's products run, instead of each thread's loads
+    // waiting in turn before every stage
+    __shared__ Z s_r[2][4][KC][TB];
+    __shared__ Z s_c[2][4][KC][TB];
+    auto issue = [&](int k0, int buf) {
+      for (int e = tid; e < 4 * KC * TB; e += NT) {
+        const int row = e % TB, kk = (e / TB) % KC, vec = e / (TB * KC);
+        const int kg = k0 + kk;
+        const bool kok = kg < nbp;
+        const int kc = kok ? kg : 0;
+        const Z* base = vec == 0 ? A + (int64_t)(p + kc) * ld
+                      : vec == 1 ? B + (int64_t)(p + kc) * ld
+                      : vec == 2 ? v.Ya + (int64_t)kc * v.ldy
+                                 : v.Yb + (int64_t)kc * v.ldy;
+        const bool rok = kok && rb + row < n, cok = kok && cb + row < n;
+        cp_async8_zfill(&s_r[buf][vec][kk][row], base + (rok ? rb + row : 0), rok);
+        cp_async8_zfill(&s_c[buf][vec][kk][row], base + (cok ? cb + row : 0), cok);
       }
-      s_r[vec][kk][row] = vr;
-      s_c[vec][kk][row] = vc;
+      cp_async_commit();
+    };
+    issue(0, 0);
+    for (int k0 = 0, st = 0; k0 < nbp; k0 += KC, ++st) {
+      const int buf = st & 1;
+      if (k0 + KC < nbp) { issue(k0 + KC, buf ^ 1); cp_async_wait<1>(); } else { cp_async_wait<0>(); }
+      __syncthreads();
+      trail_stage<Z>(s_r[buf], s_c[buf], tr, tc, accA, accB);
+      __syncthreads();  // the buffer is refilled by the issue two stages on
     }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < KC; ++kk) {
-      Z rwa[4], rwb[4], rya[4], ryb[4], cwa[4], cwb[4], cya[4], cyb[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        rwa[q] = s_r[0][kk][4 * tr + q]; rwb[q] = s_r[1][kk][4 * tr + q];
-        rya[q] = s_r[2][kk][4 * tr + q]; ryb[q] = s_r[3][kk][4 * tr + q];
-        cwa[q] = s_c[0][kk][4 * tc + q]; cwb[q] = s_c[1][kk][4 * tc + q];
-        cya[q] = s_c[2][kk][4 * tc + q]; cyb[q] = s_c[3][kk][4 * tc + q];
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          // A += wa conj(ya) + conj(wb) yb + ya conj(wa) + conj(yb) wb
-          cfmacb(accA[q][c], rwa[q], cya[c]); cfmac(accA[q][c], rwb[q], cyb[c]);
-          cfmacb(accA[q][c], rya[q], cwa[c]); cfmac(accA[q][c], ryb[q], cwb[c]);
-          // B += wb conj(ya) - conj(wa) yb + yb conj(wa) - conj(ya) wb
-          cfmacb(accB[q][c], rwb[q], cya[c]); cfmac(accB[q][c], cneg(rwa[q]), cyb[c]);
-          cfmacb(accB[q][c], ryb[q], cwa[c]); cfmac(accB[q][c], cneg(rya[q]), cwb[c]);
+  } else {
+    // [vector: wa, wb, ya, yb][kk][row]
+    __shared__ Z s_r[4][KC][TB];
+    __shared__ Z s_c[4][KC][TB];
+    for (int k0 = 0; k0 < nbp; k0 += KC) {
+      __syncthreads();
+      for (int e = tid; e < 4 * KC * TB; e += NT) {
+        const int row = e % TB, kk = (e / TB) % KC, vec = e / (TB * KC);
+        const int kg = k0 + kk;
+        Z vr = czero<Z>(), vc = czero<Z>();
+        if (kg < nbp) {
+          const int gr = rb + row, gc = cb + row;
+          if (gr < n) {
+            if (vec == 0) vr = A[gr + (int64_t)(p + kg) * ld];
+            else if (vec == 1) vr = B[gr + (int64_t)(p + kg) * ld];
+            else if (vec == 2) vr = v.Ya[gr + (int64_t)kg * v.ldy];
+            else vr = v.Yb[gr + (int64_t)kg * v.ldy];
+          }
+          if (gc < n) {
+            if (vec == 0) vc = A[gc + (int64_t)(p + kg) * ld];
+            else if (vec == 1) vc = B[gc + (int64_t)(p + kg) * ld];
+            else if (vec == 2) vc = v.Ya[gc + (int64_t)kg * v.ldy];
+            else vc = v.Yb[gc + (int64_t)kg * v.ldy];
+          }
         }
+        s_r[vec][kk][row] = vr;
+        s_c[vec][kk][row] = vc;
+      }
+      __syncthreads();
+      trail_stage<Z>(s_r, s_c, tr, tc, accA, accB);
     }
   }
 #pragma unroll
