@@ -802,6 +802,26 @@ def main():
     oz_flops = _lib.profile_flops("ozaki") / args.steps
     iters, last_corr, fell_back = solver.refine_stats()
 
+    # end to end through the host C ABI (H2D + solve + D2H inside), from and to
+    # pinned host arrays (one untimed call first: it maps the device copy of D
+    # in the stream-ordered pool). Measured right after the device-resident
+    # steps, before the FP64 comparisons heat the GPU, with its own clock record.
+    pinned_d = torch.empty((n2, n2), dtype=torch.complex128, pin_memory=True)
+    dh = pinned_d.numpy().T  # column-major (Fortran) view, ld2 = n2
+    eh = torch.zeros(n2, dtype=torch.float64, pin_memory=True).numpy()
+    e2e_ms = []
+    with ClockSampler(local) as e2e_clk:
+        for i in range(args.e2e_steps + 1):
+            dh[...] = d_host
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = solver.zquatev(n2, dh, n2, eh)
+            t1 = time.perf_counter()
+            assert rc == 0, _lib.last_error()
+            if i > 0:
+                e2e_ms.append((t1 - t0) * 1e3)
+    e2e = float(np.mean(e2e_ms))
+
     # accuracy of the last device solve (GPU residual; FP64 torch matmul as checker)
     acc = {}
     if not args.no_check:
@@ -831,23 +851,7 @@ def main():
     lib.zq_profile_enable(0)
     fprof = {k: _lib.profile_read(k) for k in ("hemv", "trail", "formq_gemm", "apply_z", "stedc", "tridiag", "formq")}
 
-    # end to end through the host C ABI (H2D + solve + D2H inside), from and to
-    # pinned host arrays (one untimed call first: it maps the device copy of D
-    # in the stream-ordered pool)
-    pinned_d = torch.empty((n2, n2), dtype=torch.complex128, pin_memory=True)
-    dh = pinned_d.numpy().T  # column-major (Fortran) view, ld2 = n2
-    eh = torch.zeros(n2, dtype=torch.float64, pin_memory=True).numpy()
-    e2e_ms = []
-    for i in range(args.e2e_steps + 1):
-        dh[...] = d_host
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        rc = solver.zquatev(n2, dh, n2, eh)
-        t1 = time.perf_counter()
-        assert rc == 0, _lib.last_error()
-        if i > 0:
-            e2e_ms.append((t1 - t0) * 1e3)
-    e2e = float(np.mean(e2e_ms))
+
 
     peaks = measured_peaks()
     bf16_peak = peaks.get("bf16_tflops_sustained") or peaks.get("bf16_tflops")
@@ -896,7 +900,7 @@ def main():
             "speedup_vs_fp64_path": fp64_ms / ms_step if ms_step > 0 else None,
             "e2e": {"value": e2e, "unit": "ms", "h2d_bytes_per_step": n2 * n * 16,
                     "d2h_bytes_per_step": n2 * n2 * 16 + n * 8, "host_memory": "pinned",
-                    "samples_ms": [round(x, 1) for x in e2e_ms]},
+                    "samples_ms": [round(x, 1) for x in e2e_ms], "clocks": e2e_clk.summary()},
             "gpu_launches": None,
             "roofline": {"bound": "tensor", "kernel": "k_oz_umma<2> (bf16 2-SM tcgen05.mma cta_group::2, M=256 N=256 per CTA pair; TMEM accumulators; TMA; Ozaki slices)",
                          "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",

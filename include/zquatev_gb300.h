@@ -101,7 +101,8 @@ int zq_zgemm_accurate(int opa, int opb, int m, int n, int k, const double* A, in
 int zquatev_device_noalloc(int n2, double* dD, int ld2, double* deig, void* stream);
 
 /* Panel width of the blocked tridiagonalisation (the reference hard-codes
- * nb = 20 at zquatev.cc:64). Valid range 1..128; default 32. */
+ * nb = 20 at zquatev.cc:64). Valid range 1..128; default 16 (the autotuned
+ * table, zq_autotune_nb, overrides it per size bucket). */
 int zq_set_block_size(int nb);
 int zq_get_block_size(void);
 

@@ -61,7 +61,9 @@ def test_argument_errors(lib):
     assert "ld2" in _lib.last_error() or "null" in _lib.last_error() or _lib.last_error() == ""
     assert lib.zq_set_block_size(0) == -5
     assert lib.zq_set_block_size(129) == -5
+    nb0 = lib.zq_get_block_size()
     assert lib.zq_set_block_size(32) == 0 and lib.zq_get_block_size() == 32
+    assert lib.zq_set_block_size(nb0) == 0
     assert lib.zq_stedc_device(-1, None, None, None, None, 1, None) == -5
     n2s = (ctypes.c_int * 1)(3)
     assert lib.zquatev_batched_device(1, n2s, n2s, None, None, None, None, None) == -5

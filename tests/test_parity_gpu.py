@@ -103,6 +103,7 @@ def test_random_sizes(gpu, n):
 
 @pytest.mark.parametrize("nb", [1, 2, 8, 16, 32, 64, 100, 128])
 def test_panel_widths(gpu, nb):
+    nb0 = gpu.zq_get_block_size()
     assert gpu.zq_set_block_size(nb) == 0
     try:
         n = 150
@@ -110,13 +111,14 @@ def test_panel_widths(gpu, nb):
         out, eig = run(d)
         check_solution(d, out, eig, n)
     finally:
-        gpu.zq_set_block_size(32)
+        gpu.zq_set_block_size(nb0)
 
 
 @pytest.mark.parametrize("nb", [16, 64, 128])
 def test_panel_widths_refined(gpu, nb):
     """The refined path's FP32 reduction (TMA-staged hemv) at panel widths up
     to 128, several panels deep, without the FP64 fallback."""
+    nb0 = gpu.zq_get_block_size()
     assert gpu.zq_set_block_size(nb) == 0
     try:
         n = 400
@@ -125,7 +127,7 @@ def test_panel_widths_refined(gpu, nb):
         assert not solver.refine_stats()[2]
         check_solution(d, out, eig, n)
     finally:
-        gpu.zq_set_block_size(32)
+        gpu.zq_set_block_size(nb0)
 
 
 def test_against_port_config0(gpu):

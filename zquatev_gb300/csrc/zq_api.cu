@@ -107,7 +107,8 @@ void prof_end(int cls, cudaStream_t st) {
 
 static std::mutex g_ctx_mu;
 static Context* g_ctx[64];
-static int g_nb = 32;   // panel width (autotuned table may override per n)
+static int g_nb = 16;   // panel width (autotuned table may override per n; 16 was fastest
+                        // for both precisions at n2 = 1024 ... 8192)
 static int g_nbq = 64;  // Q-formation block
 
 // Panel width per precision (0 FP64 path, 1 FP32 decomposition of the refined
@@ -465,6 +466,12 @@ int refined_device(Context* c, double2* dD, int64_t ldd, int n, double* deig, cu
   ra.tol = 1e-7;   // the update squares the error: |E| <= 1e-7 leaves ~1e-14
   ra.cluster_tol = 1e-13;
   ra.pair_eps = 1e-4;  // |E| <= 1e-4 from the formula: two more steps reach 1e-7
+  // After the first step a correction above 1e-6 means a pair whose gap is too
+  // small for the first-order formula to converge quadratically (seen on a
+  // random n2 = 8192 matrix: one pair's |E| stayed at 5e-5 for two steps); such
+  // pairs are rotated like clusters instead.
+  ra.pair_eps_late = 1e-6;
+  if (const char* s = getenv("ZQ_REFINE_EPS_LATE")) { const double v = atof(s); if (v > 0.0 && v < 0.5) ra.pair_eps_late = v; }
   ra.slices0 = 5;
   if (const char* s = getenv("ZQ_REFINE_SLICES0")) { const int v = atoi(s); if (v >= 3 && v <= 8) ra.slices0 = v; }
   ra.slices_res = 4;

@@ -166,7 +166,8 @@ struct RefineArgs {
   int nb, nbq, mode, max_iter;
   double tol;
   double cluster_tol;          // accepted in-cluster coupling (relative to max |lambda|)
-  double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap|
+  double pair_eps;             // first-order formula only where |coupling| <= pair_eps |gap| (first step)
+  double pair_eps_late;        // the same bound in the later steps
   int slices0;                 // Ozaki slices of the first step's products
   int slices_res;              // Ozaki slices of the products with the residual R = HX - X Lambda
   int coop;                    // the FP32 reduction may use cooperative panel launches

@@ -177,7 +177,16 @@ __global__ void k_oa_build_e(const double2* __restrict__ S1, const double2* __re
     const double2 s1 = S1[o], s2 = S2[o];
     const double2 c1 = make_double2(s1.x + lj * r1.x, s1.y + lj * r1.y);
     const double2 c2 = make_double2(s2.x + lj * r2.x, s2.y + lj * r2.y);
-    const double a1 = fmax(fabs(c1.x), fabs(c1.y)), a2 = fmax(fabs(c2.x), fabs(c2.y));
+    // The pair test is symmetric in (i, j): the transposed entry's coupling has
+    // the magnitude of S_ij + lambda_i R_ij (S1, G1 Hermitian, S2, G2
+    // antisymmetric), and testing each entry with its own lambda could flag a
+    // pair through (j, i) alone. Only i < j is recorded as a cluster pair, so
+    // that entry would take R/2 while (i, j) took the first-order value: half
+    // the pair's rotation per step (seen: |E| halving from 2.5e-5 each step).
+    const double2 c1t = make_double2(s1.x + li * r1.x, s1.y + li * r1.y);
+    const double2 c2t = make_double2(s2.x + li * r2.x, s2.y + li * r2.y);
+    const double a1 = fmax(fmax(fabs(c1.x), fabs(c1.y)), fmax(fabs(c1t.x), fabs(c1t.y)));
+    const double a2 = fmax(fmax(fabs(c2.x), fabs(c2.y)), fmax(fabs(c2t.x), fabs(c2t.y)));
     double2 e1, e2;
     bool cl = false;
     if (i == j) {
@@ -730,7 +739,7 @@ int refined_solve(RefineArgs& ra) {
       ZQ_LAUNCH_CHECK();
       ZQ_CUDA(cudaMemsetAsync(pair_count, 0, sizeof(int), st));
       k_oa_build_e<<<ne, 256, 0, st>>>(S1, S2, G1, G2, n, n, lam, part, nparts, Et, Eb, n, emax, pair_count, pairs,
-                                       pair_cap, ra.pair_eps);
+                                       pair_cap, it == 0 ? ra.pair_eps : ra.pair_eps_late);
       ZQ_LAUNCH_CHECK();
       ZQ_CUDA(cudaMemcpyAsync(hemax.data(), emax, sizeof(double) * 2 * ne, cudaMemcpyDeviceToHost, st));
       ZQ_CUDA(cudaMemcpyAsync(&hcount, pair_count, sizeof(int), cudaMemcpyDeviceToHost, st));
