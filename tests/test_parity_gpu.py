@@ -430,3 +430,27 @@ def test_refined_vs_fp64_at_scale(gpu, n2, kind):
     assert bool((v[:n, n:] == -w.conj()).all()) and bool((v[n:, n:] == u.conj()).all())
     if kind == "random":
         assert not solver.refine_stats()[2], "refined path fell back to FP64"
+
+
+@pytest.mark.parametrize("nb", [16, 32])
+def test_refined_two_steps_config1_matrix(gpu, nb):
+    """The config-1 workload's matrix converges in two refinement steps at panel
+    widths 16 and 32. At nb = 32 one pair's first-order test failed through the
+    (j, i) entry only; when the test was per entry that pair got half its
+    rotation per step and the solve took four steps (or fell back to FP64)."""
+    import torch
+
+    n = 4096
+    d = inputs.random_matrix(n, 1000)
+    dmaster = torch.from_numpy(np.ascontiguousarray(d.T)).cuda()
+    del d
+    nb0 = gpu.zq_get_block_size()
+    t0 = gpu.zq_tuned_nb(2 * n, 1)  # an autotuned width for this size would take precedence
+    assert gpu.zq_set_block_size(nb) == 0 and gpu.zq_set_tuned_nb(2 * n, 1, 0) == 0
+    try:
+        _device_solve("refined", dmaster, 2 * n)
+    finally:
+        gpu.zq_set_block_size(nb0)
+        gpu.zq_set_tuned_nb(2 * n, 1, t0)
+    iters, last, fell_back = solver.refine_stats()
+    assert not fell_back and iters == 2, (iters, last)
