@@ -192,7 +192,8 @@ int zq_profile_flops(int cls, double* flops);
  * entry points; every launch is counted on the host right after it is made). */
 long long zq_launch_count(void);
 
-/* Frees the cached device workspace of the current device. */
+/* Frees the cached device workspace of the current device, and the device copy
+ * of D that the host-memory entry points keep between calls (n2^2 complex). */
 int zq_release_workspace(void);
 
 /* ---------------------------------------------------------------- serving

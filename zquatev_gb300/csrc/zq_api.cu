@@ -148,6 +148,7 @@ void context_destroy(Context* c) {
   if (c->ws && !c->ws_external) cudaFree(c->ws);
   if (c->rb.dev && !c->rb.external) cudaFree(c->rb.dev);
   if (c->bb.dev) cudaFree(c->bb.dev);
+  if (c->hbuf) cudaFree(c->hbuf);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->st) cudaStreamDestroy(c->st);
@@ -362,12 +363,17 @@ static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors, 
   Context* c = nullptr;
   if (int rc = get_context(&c)) return rc;
   std::lock_guard<std::mutex> lk(c->mu);
-  // device copy of D: n2 x n2 with ld = n2 (plus eigenvalues)
+  // device copy of D: n2 x n2 with ld = n2 (plus eigenvalues), in the
+  // context's host-path buffer (grown on demand, kept between calls)
   const size_t dbytes = sizeof(double2) * (size_t)n2 * n2;
-  double2* dD = nullptr;
-  double* deig = nullptr;
-  ZQ_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dD), dbytes + sizeof(double) * n + 256, c->st));
-  deig = reinterpret_cast<double*>(reinterpret_cast<char*>(dD) + dbytes);
+  const size_t need = dbytes + sizeof(double) * n + 256;
+  if (c->hbuf_bytes < need) {
+    if (c->hbuf) { cudaStreamSynchronize(c->st); cudaFree(c->hbuf); c->hbuf = nullptr; c->hbuf_bytes = 0; }
+    ZQ_CUDA(cudaMalloc(&c->hbuf, need));
+    c->hbuf_bytes = need;
+  }
+  double2* dD = reinterpret_cast<double2*>(c->hbuf);
+  double* deig = reinterpret_cast<double*>(reinterpret_cast<char*>(dD) + dbytes);
   int rc = ZQ_OK;
   // ZQ_TIMING=1: host-clock time of each phase (the stream is synchronised after each)
   const char* tenv = getenv("ZQ_TIMING");
@@ -414,7 +420,6 @@ static int zquatev_host(int n2, double2* D, int ld2, double* eig, bool vectors, 
     if (e != cudaSuccess) { set_last_error(e, "cudaStreamSynchronize", __FILE__, __LINE__); rc = ZQ_ERR_CUDA; break; }
     phase("d2h");
   } while (0);
-  cudaFreeAsync(dD, c->st);
   cudaStreamSynchronize(c->st);
   return rc;
 }
@@ -767,6 +772,9 @@ int zq_release_workspace(void) {
   c->ws = nullptr;
   c->ws_bytes = 0;
   c->dc_n = -1;
+  if (c->hbuf) cudaFree(c->hbuf);
+  c->hbuf = nullptr;
+  c->hbuf_bytes = 0;
   return ZQ_OK;
 }
 

@@ -43,6 +43,11 @@ struct Context {
   // solves of this context may use cooperative launches (off for the
   // server's lanes, whose solves run beside each other)
   bool coop = true;
+  // device copy of D for the host-memory entry points, kept between calls
+  // (a 1 GB cudaMallocAsync + cudaFreeAsync per n2 = 8192 call cost ~44 ms in
+  // a process whose other allocations kept the pool from reusing the memory)
+  void* hbuf = nullptr;
+  size_t hbuf_bytes = 0;
   std::mutex mu;
 };
 
