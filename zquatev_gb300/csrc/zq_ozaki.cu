@@ -84,6 +84,16 @@ __device__ __forceinline__ void oz_entry(const OzSide& s, bool is_a, int idx, in
 }
 
 // exponent e with 2^e >= max |entry| of row/column idx (e = -1100 for a zero row)
+// max(|Re x|, |Im x|) as the bits of a non-negative double: for non-negative
+// doubles the unsigned order of the bit patterns is the order of the values,
+// so maxima are taken with integer instructions (the FP64 pipe is narrow)
+__device__ __forceinline__ unsigned long long oz_absmax_bits(double2 x) {
+  const unsigned long long mask = 0x7fffffffffffffffull;
+  const unsigned long long a = (unsigned long long)__double_as_longlong(x.x) & mask;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x.y) & mask;
+  return a > b ? a : b;
+}
+
 __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict__ exps) {
   // The entries of row/column idx over k' are Re x and Im x of each complex x
   // of the row (times s2 in A's second segment), so the maximum is taken over
@@ -98,20 +108,30 @@ __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict
     const int64_t ld = seg ? s.ld2 : s.ld1;
     const int op = seg ? s.op2 : s.op1;
     const int K = seg ? s.K2 : s.K1;
-    double m2 = 0.0;
+    unsigned long long m2 = 0;  // max |entry| as bits (sign cleared): same order as the values
+    if (K <= 0) continue;
+    // element (idx, k) of op(X) (A) or (k, idx) (B) lies at X[a + k * sk]: one
+    // branch-free address per load, so the eight loads are in flight together
+    // (loads past K read element K - 1 and are masked)
+    const bool colmaj = (op == OP_N || op == OP_R);  // op(X)(r, c) = X[r + c ld]
+    const int64_t sk = (is_a == colmaj) ? ld : 1;    // stride along k
+    const int64_t a = (is_a == colmaj) ? (int64_t)warp : (int64_t)warp * ld;
     for (int k0 = 0; k0 < K; k0 += 32 * 8) {
       double2 x[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = k0 + lane + 32 * u;
-        x[u] = make_double2(0.0, 0.0);
-        if (k < K) x[u] = is_a ? oz_op(X, ld, op, warp, k) : oz_op(X, ld, op, k, warp);
+        x[u] = __ldg(X + a + (int64_t)(k < K ? k : K - 1) * sk);
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) m2 = fmax(m2, fmax(fabs(x[u].x), fabs(x[u].y)));
+      for (int u = 0; u < 8; ++u) {
+        const bool in = k0 + lane + 32 * u < K;
+        m2 = max(m2, in ? oz_absmax_bits(x[u]) : 0ull);
+      }
     }
     // rounding is monotone: max |s2 x| = |s2| max |x| exactly
-    mx = fmax(mx, (is_a && seg) ? fabs(s.s2) * m2 : m2);
+    const double m2d = __longlong_as_double((long long)m2);
+    mx = fmax(mx, (is_a && seg) ? fabs(s.s2) * m2d : m2d);
   }
   mx = warp_max(mx);
   if (lane == 0) {
@@ -124,6 +144,26 @@ __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict
     }
     exps[warp] = e;
   }
+}
+
+// bf16 pair from its bit pattern (low half: first element)
+__device__ __forceinline__ __nv_bfloat162 oz_bf2(unsigned u) {
+  __nv_bfloat162 r;
+  *reinterpret_cast<unsigned*>(&r) = u;
+  return r;
+}
+// sign factors of a digit pair: (s0, s1) = (+-1, +-1) and (-128 s0, -128 s1)
+__device__ __forceinline__ void oz_sign_pair(bool neg0, bool neg1, __nv_bfloat162& sg, __nv_bfloat162& off) {
+  sg = oz_bf2((neg0 ? 0xBF80u : 0x3F80u) | ((neg1 ? 0xBF80u : 0x3F80u) << 16));
+  off = oz_bf2((neg0 ? 0x4300u : 0xC300u) | ((neg1 ? 0x4300u : 0xC300u) << 16));
+}
+// bf16 bits of the signed digits (s0 d0, s1 d1), d in [0, 127], without a
+// conversion instruction: the bit pattern 0x4300 | d is the bf16 value 128 + d
+// (exponent 2^7, mantissa d), and one bf16x2 FMA gives s (128 + d) - 128 s =
+// s d exactly (a zero digit gives +0)
+__device__ __forceinline__ unsigned oz_digit_pair(unsigned d0, unsigned d1, __nv_bfloat162 sg, __nv_bfloat162 off) {
+  const __nv_bfloat162 r = __hfma2(oz_bf2(0x43004300u | d0 | (d1 << 16)), sg, off);
+  return *reinterpret_cast<const unsigned*>(&r);
 }
 
 // base-128 digits of floor(|v| / 2^e * 2^(7 S)) (integer arithmetic on the
@@ -145,9 +185,9 @@ __device__ __forceinline__ unsigned long long oz_fixed(double v, int e, int F, b
 // S slices of one operand: out[t][idx][kp] (bf16), idx < padded count (zero rows above count).
 // The slices are the base-128 digits of floor(|v| / 2^e * 2^(7 S)) (integer
 // arithmetic on the 53-bit significand), with the sign of v: exact truncation.
-__global__ void k_oz_slice(OzSide s, bool is_a, int count, int count_pad, int Kp, const int* __restrict__ exps,
-                           int nsl, __nv_bfloat16* __restrict__ out_re, __nv_bfloat16* __restrict__ out_im,
-                           int64_t slice_stride) {
+__global__ void __launch_bounds__(256, 4)
+    k_oz_slice(OzSide s, bool is_a, int count, int count_pad, int Kp, const int* __restrict__ exps, int nsl,
+               __nv_bfloat16* __restrict__ out_re, __nv_bfloat16* __restrict__ out_im, int64_t slice_stride) {
   // eight consecutive k' of one row per thread (Kp is a multiple of 64), each
   // slice written as one 16-byte store
   const int64_t total8 = (int64_t)count_pad * Kp / 8;
@@ -157,34 +197,74 @@ __global__ void k_oz_slice(OzSide s, bool is_a, int count, int count_pad, int Kp
     const int idx = (int)(t / Kp), kp0 = (int)(t % Kp);
     const bool live = idx < count;
     const int e = live ? exps[idx] : 0;
+    double va[8], vb[8];
+    // the eight k' lie in one half (Re or Im part) of one segment in all but
+    // the groups that straddle a boundary or the padding: there the eight
+    // loads use one base and one stride and are issued together
+    int seg = 0, k = kp0;
+    if (k >= 2 * s.K1) { seg = 1; k -= 2 * s.K1; }
+    const int K = seg ? s.K2 : s.K1;
+    const bool imag_half = k >= K;
+    const int kk0 = imag_half ? k - K : k;
+    if (live && kk0 + 7 < K) {
+      const double2* X = seg ? s.X2 : s.X1;
+      const int64_t ld = seg ? s.ld2 : s.ld1;
+      const int op = seg ? s.op2 : s.op1;
+      const bool colmaj = (op == OP_N || op == OP_R);
+      const int64_t sk = (is_a == colmaj) ? ld : 1;
+      const double2* p = X + ((is_a == colmaj) ? (int64_t)idx : (int64_t)idx * ld) + (int64_t)kk0 * sk;
+      const double cs = (op == OP_R || op == OP_C) ? -1.0 : 1.0;  // sign of the imaginary part of op(X)
+      double2 x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x[u] = __ldg(p + u * sk);
+      if (is_a) {
+        const double sg = seg ? s.s2 : 1.0;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          va[u] = imag_half ? (sg * cs) * x[u].y : sg * x[u].x;
+          vb[u] = 0.0;
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const double y = cs * x[u].y;
+          va[u] = imag_half ? -y : x[u].x;  // Bre = [br | -bi]
+          vb[u] = imag_half ? x[u].x : y;   // Bim = [bi | br]
+        }
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        va[u] = 0.0;
+        vb[u] = 0.0;
+        if (live) oz_entry(s, is_a, idx, kp0 + u, va[u], vb[u]);
+      }
+    }
     unsigned long long V0[8], V1[8];
     unsigned n0 = 0, n1 = 0;  // sign bits
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
-      double a = 0.0, b = 0.0;
-      if (live) oz_entry(s, is_a, idx, kp0 + u, a, b);
       bool ng0, ng1;
-      V0[u] = oz_fixed(a, e, F, ng0);
-      V1[u] = oz_fixed(b, e, F, ng1);
+      V0[u] = oz_fixed(va[u], e, F, ng0);
+      V1[u] = oz_fixed(vb[u], e, F, ng1);
       n0 |= (unsigned)ng0 << u;
       n1 |= (unsigned)ng1 << u;
+    }
+    __nv_bfloat162 sg0[4], of0[4], sg1[4], of1[4];
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+      oz_sign_pair((n0 >> (2 * h)) & 1, (n0 >> (2 * h + 1)) & 1, sg0[h], of0[h]);
+      oz_sign_pair((n1 >> (2 * h)) & 1, (n1 >> (2 * h + 1)) & 1, sg1[h], of1[h]);
     }
     for (int q = 0; q < nsl; ++q) {
       const int shift = F - OZ_BETA * (q + 1);
       unsigned pr[4], pi[4];
 #pragma unroll
       for (int h = 0; h < 4; ++h) {
-        unsigned short lo, hi;
-        int d = (int)((V0[2 * h] >> shift) & 127);
-        lo = __bfloat16_as_ushort(__int2bfloat16_rn(((n0 >> (2 * h)) & 1) ? -d : d));
-        d = (int)((V0[2 * h + 1] >> shift) & 127);
-        hi = __bfloat16_as_ushort(__int2bfloat16_rn(((n0 >> (2 * h + 1)) & 1) ? -d : d));
-        pr[h] = (unsigned)lo | ((unsigned)hi << 16);
-        d = (int)((V1[2 * h] >> shift) & 127);
-        lo = __bfloat16_as_ushort(__int2bfloat16_rn(((n1 >> (2 * h)) & 1) ? -d : d));
-        d = (int)((V1[2 * h + 1] >> shift) & 127);
-        hi = __bfloat16_as_ushort(__int2bfloat16_rn(((n1 >> (2 * h + 1)) & 1) ? -d : d));
-        pi[h] = (unsigned)lo | ((unsigned)hi << 16);
+        pr[h] = oz_digit_pair((unsigned)(V0[2 * h] >> shift) & 127u, (unsigned)(V0[2 * h + 1] >> shift) & 127u, sg0[h],
+                              of0[h]);
+        pi[h] = oz_digit_pair((unsigned)(V1[2 * h] >> shift) & 127u, (unsigned)(V1[2 * h + 1] >> shift) & 127u, sg1[h],
+                              of1[h]);
       }
       *reinterpret_cast<uint4*>(out_re + q * slice_stride + t) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
       if (out_im) *reinterpret_cast<uint4*>(out_im + q * slice_stride + t) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
@@ -211,28 +291,28 @@ __global__ void k_oz_exp_cm(OzSide s, int count, int Kc, int* __restrict__ exps)
   const int kb = blockIdx.y * 256;
   double mx = 0.0;
   if (row < count) {
-    for (int q0 = ty; q0 < 256; q0 += 8 * 8) {
-      double2 x[8];
-      double sc[8];
+    // this CTA's columns [kb, kb + 256) of each segment: X[row + k ld], one
+    // base and stride per segment, eight loads in flight per thread (loads
+    // past the range read its last column and are masked)
+    for (int seg = 0; seg < 2; ++seg) {
+      const double2* X = seg ? s.X2 : s.X1;
+      const int K = seg ? s.K2 : s.K1;
+      const int koff = seg ? s.K1 : 0;
+      const int lo = max(kb, koff) - koff, hi = min(min(kb + 256, Kc), koff + K) - koff;
+      if (X == nullptr || lo >= hi) continue;
+      const int64_t ld = seg ? s.ld2 : s.ld1;
+      const double2* p = X + row;
+      unsigned long long m2 = 0;
+      for (int q0 = lo + ty; q0 < hi; q0 += 8 * 8) {
+        double2 x[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int k = kb + q0 + 8 * u;
-        x[u] = make_double2(0.0, 0.0);
-        sc[u] = 1.0;
-        if (q0 + 8 * u < 256 && k < Kc) {
-          if (k < s.K1) {
-            x[u] = oz_op(s.X1, s.ld1, s.op1, row, k);
-          } else {
-            x[u] = oz_op(s.X2, s.ld2, s.op2, row, k - s.K1);
-            sc[u] = fabs(s.s2);
-          }
-        }
-      }
+        for (int u = 0; u < 8; ++u) x[u] = __ldg(p + (int64_t)min(q0 + 8 * u, hi - 1) * ld);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const double m = fmax(fabs(x[u].x), fabs(x[u].y));
-        mx = fmax(mx, sc[u] == 1.0 ? m : sc[u] * m);
+        for (int u = 0; u < 8; ++u) m2 = max(m2, q0 + 8 * u < hi ? oz_absmax_bits(x[u]) : 0ull);
       }
+      // rounding is monotone: max |s2 x| = |s2| max |x| exactly
+      const double m2d = __longlong_as_double((long long)m2);
+      mx = fmax(mx, seg ? fabs(s.s2) * m2d : m2d);
     }
   }
   s_m[ty][tx] = mx;
