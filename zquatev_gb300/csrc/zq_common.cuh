@@ -87,6 +87,18 @@ template <typename T> __device__ __forceinline__ T warp_max(T v) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+// |v| as the bits of a non-negative double, and max(|Re x|, |Im x|) likewise:
+// for non-negative doubles the unsigned order of the bit patterns is the order
+// of the values, so running maxima can use integer instructions (GB300's FP64
+// pipe is narrow); __longlong_as_double turns the result back into |v|
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long absmax_bits(double2 x) {
+  const unsigned long long a = abs_bits(x.x), b = abs_bits(x.y);
+  return a > b ? a : b;
+}
+__device__ __forceinline__ double bits_to_double(unsigned long long b) { return __longlong_as_double((long long)b); }
 // Sum over the block; every thread gets the result. `sh` needs blockDim/32 slots.
 template <typename T> __device__ T block_sum(T v, T* sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;

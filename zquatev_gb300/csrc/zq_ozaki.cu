@@ -84,16 +84,6 @@ __device__ __forceinline__ void oz_entry(const OzSide& s, bool is_a, int idx, in
 }
 
 // exponent e with 2^e >= max |entry| of row/column idx (e = -1100 for a zero row)
-// max(|Re x|, |Im x|) as the bits of a non-negative double: for non-negative
-// doubles the unsigned order of the bit patterns is the order of the values,
-// so maxima are taken with integer instructions (the FP64 pipe is narrow)
-__device__ __forceinline__ unsigned long long oz_absmax_bits(double2 x) {
-  const unsigned long long mask = 0x7fffffffffffffffull;
-  const unsigned long long a = (unsigned long long)__double_as_longlong(x.x) & mask;
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x.y) & mask;
-  return a > b ? a : b;
-}
-
 __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict__ exps) {
   // The entries of row/column idx over k' are Re x and Im x of each complex x
   // of the row (times s2 in A's second segment), so the maximum is taken over
@@ -126,11 +116,11 @@ __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const bool in = k0 + lane + 32 * u < K;
-        m2 = max(m2, in ? oz_absmax_bits(x[u]) : 0ull);
+        m2 = max(m2, in ? absmax_bits(x[u]) : 0ull);
       }
     }
     // rounding is monotone: max |s2 x| = |s2| max |x| exactly
-    const double m2d = __longlong_as_double((long long)m2);
+    const double m2d = bits_to_double(m2);
     mx = fmax(mx, (is_a && seg) ? fabs(s.s2) * m2d : m2d);
   }
   mx = warp_max(mx);
@@ -308,10 +298,10 @@ __global__ void k_oz_exp_cm(OzSide s, int count, int Kc, int* __restrict__ exps)
 #pragma unroll
         for (int u = 0; u < 8; ++u) x[u] = __ldg(p + (int64_t)min(q0 + 8 * u, hi - 1) * ld);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) m2 = max(m2, q0 + 8 * u < hi ? oz_absmax_bits(x[u]) : 0ull);
+        for (int u = 0; u < 8; ++u) m2 = max(m2, q0 + 8 * u < hi ? absmax_bits(x[u]) : 0ull);
       }
       // rounding is monotone: max |s2 x| = |s2| max |x| exactly
-      const double m2d = __longlong_as_double((long long)m2);
+      const double m2d = bits_to_double(m2);
       mx = fmax(mx, seg ? fabs(s.s2) * m2d : m2d);
     }
   }
@@ -563,31 +553,68 @@ size_t ozaki_workspace_bytes(int nq) {
 
 // structured square outputs: fill the upper triangle from the lower one
 // (sym = +1 Hermitian, -1 complex antisymmetric); diagonal 64-tiles averaged
-__global__ void k_oz_symfill(double2* __restrict__ C, int64_t ldc, int n, int sym) {
-  const int64_t total = (int64_t)n * n;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % n), j = (int)(t / n);
-    if (i < j) continue;
-    const int64_t oij = i + (int64_t)j * ldc, oji = j + (int64_t)i * ldc;
-    double2 a = C[oij];
-    if ((i >> 6) == (j >> 6)) {
-      const double2 b = C[oji];
+// 32 x 32 tiles: the block of tile pair (ti >= tj) reads the lower tile and,
+// inside the diagonal 64 x 64 blocks (computed in full by the product), the
+// mirrored upper tile, and writes both, all with coalesced rows; the mirror
+// is transposed through shared memory.
+constexpr int SF_T = 32;
+__global__ void __launch_bounds__(256) k_oz_symfill(double2* __restrict__ C, int64_t ldc, int n, int sym) {
+  const int ti = blockIdx.x, tj = blockIdx.y;
+  if (tj > ti) return;
+  __shared__ double2 sl[SF_T][SF_T + 1];  // sl[r][c] = C(i0 + r, j0 + c)
+  __shared__ double2 su[SF_T][SF_T + 1];  // su[r][c] = C(j0 + r, i0 + c)
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = ti * SF_T, j0 = tj * SF_T;
+  const bool diag64 = (ti >> 1) == (tj >> 1);  // the tile pair lies in a diagonal 64 x 64 block
+#pragma unroll
+  for (int k = 0; k < SF_T / 8; ++k) {
+    const int c = ty + 8 * k;
+    if (i0 + tx < n && j0 + c < n) sl[tx][c] = C[(i0 + tx) + (int64_t)(j0 + c) * ldc];
+    if (diag64 && j0 + tx < n && i0 + c < n) su[tx][c] = C[(j0 + tx) + (int64_t)(i0 + c) * ldc];
+  }
+  __syncthreads();
+  // entry (i, j) = (i0 + r, j0 + c), i >= j: its value, written back below, and
+  // its mirror, staged for the upper tile (threads own distinct (r, c), so the
+  // writes to su go to entries no other thread reads)
+  double2 mir[SF_T / 8];
+#pragma unroll
+  for (int k = 0; k < SF_T / 8; ++k) {
+    const int r = tx, c = ty + 8 * k;
+    const int i = i0 + r, j = j0 + c;
+    mir[k] = make_double2(0.0, 0.0);
+    if (i >= n || j >= n || i < j) continue;
+    double2 a = sl[r][c];
+    if (diag64) {
+      const double2 b = su[c][r];  // C(j, i)
       if (sym > 0) a = make_double2(0.5 * (a.x + b.x), 0.5 * (a.y - b.y));
       else a = make_double2(0.5 * (a.x - b.x), 0.5 * (a.y - b.y));
     }
     if (i == j) {
       if (sym > 0) a.y = 0.0; else a = make_double2(0.0, 0.0);
     }
-    C[oij] = a;
-    C[oji] = (sym > 0) ? make_double2(a.x, -a.y) : make_double2(-a.x, -a.y);
+    C[i + (int64_t)j * ldc] = a;
+    mir[k] = (sym > 0) ? make_double2(a.x, -a.y) : make_double2(-a.x, -a.y);
+  }
+  __syncthreads();  // every read of su is done
+#pragma unroll
+  for (int k = 0; k < SF_T / 8; ++k) {
+    const int r = tx, c = ty + 8 * k;
+    su[c][r] = mir[k];
+  }
+  __syncthreads();
+  // upper tile: C(j0 + r, i0 + c) for i0 + c > j0 + r
+#pragma unroll
+  for (int k = 0; k < SF_T / 8; ++k) {
+    const int r = tx, c = ty + 8 * k;
+    const int row = j0 + r, col = i0 + c;
+    if (row < n && col < n && col > row) C[row + (int64_t)col * ldc] = su[r][c];
   }
 }
 
 int structured_fill(double2* C, int64_t ldc, int n, int sym, cudaStream_t st) {
   if (n <= 0) return ZQ_OK;
-  const int64_t total = (int64_t)n * n;
-  const int blocks = (int)((total + 255) / 256 > 16384 ? 16384 : (total + 255) / 256);
-  k_oz_symfill<<<blocks, 256, 0, st>>>(C, ldc, n, sym);
+  const unsigned nt = (unsigned)ceil_div(n, SF_T);
+  k_oz_symfill<<<dim3(nt, nt), dim3(SF_T, 8), 0, st>>>(C, ldc, n, sym);
   ZQ_LAUNCH_CHECK();
   return ZQ_OK;
 }
@@ -699,8 +726,7 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
     ZQ_LAUNCH_CHECK();
   }
   if (opt.structured != 0 && !opt.nofill) {
-    k_oz_symfill<<<grid((int64_t)m * n), 256, 0, st>>>(g.C, g.ldc, m, opt.structured);
-    ZQ_LAUNCH_CHECK();
+    if (int rc = structured_fill(g.C, g.ldc, m, opt.structured, st)) return rc;
   }
   return ZQ_OK;
 }

@@ -117,7 +117,8 @@ __global__ void k_oa_norms(const double2* __restrict__ S1, const double2* __rest
                            const double2* __restrict__ G2, int64_t ld, int n, const double* __restrict__ lam,
                            double* __restrict__ part) {
   __shared__ double sh[32];
-  double ss = 0.0, rr = 0.0, lm = 0.0;
+  unsigned long long ssb = 0, rrb = 0;  // maxima as bits (integer instructions)
+  double lm = 0.0;
   const int64_t total = (int64_t)n * n;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % n), j = (int)(t / n);
@@ -125,12 +126,12 @@ __global__ void k_oa_norms(const double2* __restrict__ S1, const double2* __rest
     double2 s1 = S1[o], g1 = G1[o];
     if (i == j) { s1.x -= lam[j]; g1.x -= 1.0; }
     const double2 s2 = S2[o], g2 = G2[o];
-    ss = fmax(ss, fmax(fmax(fabs(s1.x), fabs(s1.y)), fmax(fabs(s2.x), fabs(s2.y))));
-    rr = fmax(rr, fmax(fmax(fabs(g1.x), fabs(g1.y)), fmax(fabs(g2.x), fabs(g2.y))));
+    ssb = max(ssb, max(absmax_bits(s1), absmax_bits(s2)));
+    rrb = max(rrb, max(absmax_bits(g1), absmax_bits(g2)));
     if (i == 0) lm = fmax(lm, fabs(lam[j]));
   }
-  ss = block_max(ss, sh);
-  rr = block_max(rr, sh);
+  const double ss = block_max(bits_to_double(ssb), sh);
+  const double rr = block_max(bits_to_double(rrb), sh);
   lm = block_max(lm, sh);
   if (threadIdx.x == 0) {
     part[3 * blockIdx.x + 0] = ss;
