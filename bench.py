@@ -111,12 +111,20 @@ class ClockSampler:
         self.proc = None
 
     def __enter__(self):
+        # the sampler's start-up (driver and NVML initialisation) is kept out of
+        # the timed region: wait (at most 5 s) for its first sample
+        self.first = []
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
+        if self.proc is not None:
+            import select
+            ready, _, _ = select.select([self.proc.stdout], [], [], 5.0)
+            if ready:
+                self.first.append(self.proc.stdout.readline())
         return self
 
     def __exit__(self, *a):
@@ -128,7 +136,7 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
                 out = ""
-            self.lines = [l for l in out.splitlines() if l.strip()]
+            self.lines = [l for l in self.first + out.splitlines() if l.strip()]
 
     def summary(self):
         sm, mx, reasons = [], None, set()
