@@ -84,13 +84,18 @@ __device__ __forceinline__ void oz_entry(const OzSide& s, bool is_a, int idx, in
 }
 
 // exponent e with 2^e >= max |entry| of row/column idx (e = -1100 for a zero row)
-__global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict__ exps) {
+__global__ void k_oz_exp(OzSide s, bool is_a, int count, int parts, int* __restrict__ exps) {
   // The entries of row/column idx over k' are Re x and Im x of each complex x
   // of the row (times s2 in A's second segment), so the maximum is taken over
-  // max(|Re x|, |Im x|) in one pass with eight loads in flight per lane.
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (warp >= count) return;
-  (void)Kp;
+  // max(|Re x|, |Im x|) with eight loads in flight per lane. One warp per
+  // (row/column, part): part p takes the chunks p, p + parts, ... of 256
+  // entries of each segment, so that enough warps are resident to cover the
+  // load latency. The frexp exponent is monotone in the value, so the largest
+  // part exponent (atomicMax into exps, preset to -1100: a zero row) is the
+  // exponent of the maximum.
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (gw >= count * parts) return;
+  const int warp = gw / parts, part = gw - warp * parts;
   double mx = 0.0;
   const int nseg = (s.X2 != nullptr && s.K2 > 0) ? 2 : 1;
   for (int seg = 0; seg < nseg; ++seg) {
@@ -106,7 +111,7 @@ __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict
     const bool colmaj = (op == OP_N || op == OP_R);  // op(X)(r, c) = X[r + c ld]
     const int64_t sk = (is_a == colmaj) ? ld : 1;    // stride along k
     const int64_t a = (is_a == colmaj) ? (int64_t)warp : (int64_t)warp * ld;
-    for (int k0 = 0; k0 < K; k0 += 32 * 8) {
+    for (int k0 = part * 256; k0 < K; k0 += parts * 256) {
       double2 x[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -124,15 +129,10 @@ __global__ void k_oz_exp(OzSide s, bool is_a, int count, int Kp, int* __restrict
     mx = fmax(mx, (is_a && seg) ? fabs(s.s2) * m2d : m2d);
   }
   mx = warp_max(mx);
-  if (lane == 0) {
-    int e = -1100;
-    if (mx > 0.0) {
-      int ex;
-      const double f = frexp(mx, &ex);  // mx = f 2^ex, f in [0.5, 1)
-      e = ex;                           // 2^ex > mx
-      (void)f;
-    }
-    exps[warp] = e;
+  if (lane == 0 && mx > 0.0) {
+    int ex;
+    frexp(mx, &ex);  // mx = f 2^ex, f in [0.5, 1): 2^ex > mx
+    atomicMax(exps + warp, ex);
   }
 }
 
@@ -619,6 +619,15 @@ int structured_fill(double2* C, int64_t ldc, int n, int sym, cudaStream_t st) {
   return ZQ_OK;
 }
 
+// warps per row/column of k_oz_exp: enough for about 48 resident warps per
+// SM (152 SMs), at most 8, and at least two 256-entry chunks per warp
+static int oz_exp_parts(int count, const OzSide& s) {
+  const int kmax = s.K1 > s.K2 ? s.K1 : s.K2;
+  int parts = 1;
+  while (parts < 8 && (int64_t)count * parts < 152 * 48 && kmax >= 2 * 256 * parts) parts *= 2;
+  return parts;
+}
+
 int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st,
                 const OzOpts& opt) {
   const int m = g.m, n = g.n;
@@ -665,14 +674,22 @@ int zgemm_ozaki(int opa1, int opb1, int opa2, int opb2, const ZgemmArgs& g, void
                                                                                                         nsl, As, mp * Kp);
       ZQ_LAUNCH_CHECK();
     } else {
-      k_oz_exp<<<ceil_div(m * 32, 256), 256, 0, st>>>(a, true, m, (int)Kp, ea);
+      const int parts = oz_exp_parts(m, a);
+      k_oz_exp_init<<<ceil_div(m, 256), 256, 0, st>>>(ea, m);
+      ZQ_LAUNCH_CHECK();
+      k_oz_exp<<<ceil_div(m * parts * 32, 256), 256, 0, st>>>(a, true, m, parts, ea);
       ZQ_LAUNCH_CHECK();
       k_oz_slice<<<grid(mp * Kp / 8), 256, 0, st>>>(a, true, m, (int)mp, (int)Kp, ea, nsl, As, nullptr, mp * Kp);
       ZQ_LAUNCH_CHECK();
     }
   }
-  k_oz_exp<<<ceil_div(n * 32, 256), 256, 0, st>>>(b, false, n, (int)Kp, eb);
-  ZQ_LAUNCH_CHECK();
+  {
+    const int parts = oz_exp_parts(n, b);
+    k_oz_exp_init<<<ceil_div(n, 256), 256, 0, st>>>(eb, n);
+    ZQ_LAUNCH_CHECK();
+    k_oz_exp<<<ceil_div(n * parts * 32, 256), 256, 0, st>>>(b, false, n, parts, eb);
+    ZQ_LAUNCH_CHECK();
+  }
   k_oz_slice<<<grid(np * Kp / 8), 256, 0, st>>>(b, false, n, (int)np, (int)Kp, eb, nsl, Brs, Bis, np * Kp);
   ZQ_LAUNCH_CHECK();
   OzGemmArgs og{};
