@@ -241,9 +241,15 @@ static int formq_kblocks_per_split() {
   return v;
 }
 
+// split-K partials of the look-ahead stream's Gram products (complex elements)
+static int64_t fq_hcap(int nbq) { return (int64_t)64 * nbq * nbq; }
+
 size_t form_q_workspace_bytes(int n, int nbq) {
-  // Wa, Wb (n x nbq), G1, G2, Ta, Tb (nbq^2), C1e, C1o, C2e, C2o (nbq x n), split-K partials
-  return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n + (size_t)fq_pcap(n, nbq)) + 256;
+  // Wa, Wb (n x nbq), G1, G2, Ta, Tb (nbq^2), C1e, C1o, C2e, C2o (nbq x n), split-K partials;
+  // then the look-ahead slot: Wa, Wb, G1, G2, Ta, Tb and its Gram products' partials
+  return sizeof(double2) * ((size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + 4 * (size_t)nbq * n + (size_t)fq_pcap(n, nbq) +
+                            (size_t)2 * n * nbq + 4 * (size_t)nbq * nbq + (size_t)fq_hcap(nbq)) +
+         256;
 }
 
 // Operand source of the tensor-core product (zq_tc32.cu) over a complex64 array.
@@ -267,43 +273,58 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
   ZQ_LAUNCH_CHECK();
   const int nref = n - 2;  // reflectors exist for columns 0..n-3
   if (nref <= 0) return ZQ_OK;
+  // Per block: W (the block's reflectors, packed), its Gram matrices G1, G2
+  // and T depend only on the reflectors, not on X; they form a slot. In the
+  // FP32 path the next block's slot is prepared on a look-ahead stream while
+  // this block's products with X run (two slots, events in both directions).
+  struct Slot { Z *Wa, *Wb, *G1, *G2, *Ta, *Tb; };
   Z* p = reinterpret_cast<Z*>(ws);
-  Z* Wa = p; p += (size_t)n * nbq;
-  Z* Wb = p; p += (size_t)n * nbq;
-  Z* G1 = p; p += (size_t)nbq * nbq;
-  Z* G2 = p; p += (size_t)nbq * nbq;
-  Z* Ta = p; p += (size_t)nbq * nbq;
-  Z* Tb = p; p += (size_t)nbq * nbq;
+  Slot slot[2];
+  slot[0].Wa = p; p += (size_t)n * nbq;
+  slot[0].Wb = p; p += (size_t)n * nbq;
+  slot[0].G1 = p; p += (size_t)nbq * nbq;
+  slot[0].G2 = p; p += (size_t)nbq * nbq;
+  slot[0].Ta = p; p += (size_t)nbq * nbq;
+  slot[0].Tb = p; p += (size_t)nbq * nbq;
   Z* C1e = p; p += (size_t)nbq * n;
   Z* C1o = p; p += (size_t)nbq * n;
   Z* C2e = p; p += (size_t)nbq * n;
   Z* C2o = p; p += (size_t)nbq * n;
   Z* Pk = p;
   const int64_t pcap = fq_pcap(n, nbq);
+  p += pcap;
+  slot[1].Wa = p; p += (size_t)n * nbq;
+  slot[1].Wb = p; p += (size_t)n * nbq;
+  slot[1].G1 = p; p += (size_t)nbq * nbq;
+  slot[1].G2 = p; p += (size_t)nbq * nbq;
+  slot[1].Ta = p; p += (size_t)nbq * nbq;
+  slot[1].Tb = p; p += (size_t)nbq * nbq;
+  Z* Ph = p;
+  const int64_t hcap = fq_hcap(nbq);
   Z* Xa = X;
   Z* Xb = X + n;
   Z one = czero<Z>(), zero = czero<Z>(), mone = czero<Z>();
   one.x = 1; mone.x = -1;
   const int nblocks = ceil_div(nref, nbq);
-  for (int bi = nblocks - 1; bi >= 0; --bi) {
+  // pack W of block bi, its Gram matrices and T into s, on stream sp
+  auto prep = [&](int bi, const Slot& s, cudaStream_t sp, Z* P, int64_t pc) -> int {
     const int pb = bi * nbq;
     const int kb = (nbq < nref - pb) ? nbq : (nref - pb);
     const int L = n - 1 - pb;
-    k_pack_w<Z><<<ceil_div(L * kb, 256) > 2048 ? 2048 : ceil_div(L * kb, 256), 256, 0, st>>>(M, ldm, n, pb, kb, L, Wa, Wb);
+    k_pack_w<Z><<<ceil_div(L * kb, 256) > 2048 ? 2048 : ceil_div(L * kb, 256), 256, 0, sp>>>(M, ldm, n, pb, kb, L, s.Wa,
+                                                                                           s.Wb);
     ZQ_LAUNCH_CHECK();
-    Args g{};
-    g.P = Pk; g.pcap = pcap;
     // G1 = Wa^H Wa + Wb^H Wb ; G2 = Wa^T Wb - Wb^T Wa   (kb x kb, inner L)
-    g = Args{};
-    g.P = Pk; g.pcap = pcap;
+    Args g{};
+    g.P = P; g.pcap = pc;
     g.m = kb; g.n = kb; g.k1 = L; g.k2 = L;
-    g.A1 = Wa; g.lda1 = L; g.B1 = Wa; g.ldb1 = L;
-    g.A2 = Wb; g.lda2 = L; g.B2 = Wb; g.ldb2 = L;
+    g.A1 = s.Wa; g.lda1 = L; g.B1 = s.Wa; g.ldb1 = L;
+    g.A2 = s.Wb; g.lda2 = L; g.B2 = s.Wb; g.ldb2 = L;
     g.s2 = (R)1; g.alpha = one; g.beta = zero;
-    g.C = G1; g.ldc = kb;
-    if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, st)) return rc;
-    g.A1 = Wa; g.B1 = Wb; g.A2 = Wb; g.B2 = Wa; g.s2 = (R)-1; g.C = G2;
-    if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, st)) return rc;
+    g.C = s.G1; g.ldc = kb;
+    if (int rc = zgemm(OP_C, OP_N, OP_C, OP_N, g, 1, sp)) return rc;
+    g.A1 = s.Wa; g.B1 = s.Wb; g.A2 = s.Wb; g.B2 = s.Wa; g.s2 = (R)-1; g.C = s.G2;
+    if (int rc = zgemm(OP_T, OP_N, OP_T, OP_N, g, 1, sp)) return rc;
     if constexpr (std::is_same<R, float>::value) {
       const size_t sm = sizeof(float2) * 4 * (size_t)kb * kb;  // kb <= 64: <= 128 KB
       static std::atomic<unsigned long long> attr_set{0};  // per device
@@ -314,11 +335,63 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
         ZQ_CUDA(cudaFuncSetAttribute(k_build_t_sm, cudaFuncAttributeMaxDynamicSharedMemorySize, 4 * 64 * 64 * 8));
         attr_set.fetch_or(bit);
       }
-      k_build_t_sm<<<1, 1024, sm, st>>>(G1, G2, kb, Ta, Tb);
+      k_build_t_sm<<<1, 1024, sm, sp>>>(s.G1, s.G2, kb, s.Ta, s.Tb);
     } else {
-      k_build_t<Z><<<1, 1024, 0, st>>>(G1, G2, kb, Ta, Tb);
+      k_build_t<Z><<<1, 1024, 0, sp>>>(s.G1, s.G2, kb, s.Ta, s.Tb);
     }
     ZQ_LAUNCH_CHECK();
+    return ZQ_OK;
+  };
+  // look-ahead stream and its events (FP32 path, more than one block)
+  const bool ahead = fp32 && nblocks > 1;
+  cudaStream_t sh = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  struct Release {
+    cudaStream_t& sh; cudaEvent_t& f; cudaEvent_t* r; cudaEvent_t* w;
+    ~Release() {
+      // safe with work pending: resources are released once it completes
+      for (int i = 0; i < 2; ++i) { if (r[i]) cudaEventDestroy(r[i]); if (w[i]) cudaEventDestroy(w[i]); }
+      if (f) cudaEventDestroy(f);
+      if (sh) cudaStreamDestroy(sh);
+    }
+  } release{sh, ev_fork, ev_ready, ev_free};
+  if (ahead) {
+    ZQ_CUDA(cudaStreamCreateWithFlags(&sh, cudaStreamNonBlocking));
+    ZQ_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i) {
+      ZQ_CUDA(cudaEventCreateWithFlags(&ev_ready[i], cudaEventDisableTiming));
+      ZQ_CUDA(cudaEventCreateWithFlags(&ev_free[i], cudaEventDisableTiming));
+    }
+    // the look-ahead stream starts after everything already queued on st
+    ZQ_CUDA(cudaEventRecord(ev_fork, st));
+    ZQ_CUDA(cudaStreamWaitEvent(sh, ev_fork, 0));
+    const int b0 = nblocks - 1;
+    if (int rc = prep(b0, slot[b0 & 1], sh, Ph, hcap)) return rc;
+    ZQ_CUDA(cudaEventRecord(ev_ready[b0 & 1], sh));
+  }
+  for (int bi = nblocks - 1; bi >= 0; --bi) {
+    const int pb = bi * nbq;
+    const int kb = (nbq < nref - pb) ? nbq : (nref - pb);
+    const int L = n - 1 - pb;
+    const int si = ahead ? (bi & 1) : 0;
+    const Slot& cur = slot[si];
+    if (ahead) {
+      if (bi >= 1) {
+        // next block into the other slot, once the block that used it last
+        // (bi + 1) has finished its X update
+        if (bi + 1 <= nblocks - 1) ZQ_CUDA(cudaStreamWaitEvent(sh, ev_free[si ^ 1], 0));
+        if (int rc = prep(bi - 1, slot[si ^ 1], sh, Ph, hcap)) return rc;
+        ZQ_CUDA(cudaEventRecord(ev_ready[si ^ 1], sh));
+      }
+      ZQ_CUDA(cudaStreamWaitEvent(st, ev_ready[si], 0));
+    } else {
+      if (int rc = prep(bi, cur, st, Pk, pcap)) return rc;
+    }
+    Z* const Wa = cur.Wa;
+    Z* const Wb = cur.Wb;
+    Z* const Ta = cur.Ta;
+    Z* const Tb = cur.Tb;
+    Args g{};
     // C1e = Wa^H Xa_sub + Wb^H Xb_sub ; C1o = Wa^T Xb_sub - Wb^T Xa_sub   (kb x L)
     Z* Xas = Xa + (pb + 1) + (int64_t)(pb + 1) * ldx;
     Z* Xbs = Xb + (pb + 1) + (int64_t)(pb + 1) * ldx;
@@ -406,6 +479,7 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
           if (rc) return rc;
         }
       }
+      if (ahead) ZQ_CUDA(cudaEventRecord(ev_free[si], st));  // this slot may be refilled
       continue;
     }
     g = Args{};
@@ -418,6 +492,7 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
     g.A1 = Wb; g.A2 = Wa; g.s2 = (R)1; g.C = Xbs;
     if (int rc = zgemm(OP_N, OP_N, OP_R, OP_N, g, 1, st)) return rc;
+    if (ahead) ZQ_CUDA(cudaEventRecord(ev_free[si], st));  // this slot may be refilled
   }
   return ZQ_OK;
 }
