@@ -343,7 +343,7 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
     return ZQ_OK;
   };
   // look-ahead stream and its events (FP32 path, more than one block)
-  const bool ahead = fp32 && nblocks > 1;
+  bool ahead = fp32 && nblocks > 1;
   cudaStream_t sh = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   struct Release {
@@ -356,12 +356,19 @@ int form_q(const cplx<R>* M, int64_t ldm, int n, const double* phi, cplx<R>* X, 
     }
   } release{sh, ev_fork, ev_ready, ev_free};
   if (ahead) {
-    ZQ_CUDA(cudaStreamCreateWithFlags(&sh, cudaStreamNonBlocking));
-    ZQ_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-    for (int i = 0; i < 2; ++i) {
-      ZQ_CUDA(cudaEventCreateWithFlags(&ev_ready[i], cudaEventDisableTiming));
-      ZQ_CUDA(cudaEventCreateWithFlags(&ev_free[i], cudaEventDisableTiming));
+    // without the stream or its events (resources exhausted) the blocks run
+    // one after another on st, as in the FP64 path
+    bool ok = cudaStreamCreateWithFlags(&sh, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; ++i)
+      ok = cudaEventCreateWithFlags(&ev_ready[i], cudaEventDisableTiming) == cudaSuccess &&
+           cudaEventCreateWithFlags(&ev_free[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      (void)cudaGetLastError();
+      ahead = false;
     }
+  }
+  if (ahead) {
     // the look-ahead stream starts after everything already queued on st
     ZQ_CUDA(cudaEventRecord(ev_fork, st));
     ZQ_CUDA(cudaStreamWaitEvent(sh, ev_fork, 0));
